@@ -1,0 +1,422 @@
+// bf_api.cu -- host side of the C ABI declared in include/beamform.h.
+//
+// Owns the per-device state (error word, staging and operand scratch), picks
+// the kernel family, and implements the drop-in form_beams() of cpu.cxx:15-16
+// on top of the explicit entry points.  No entry point exits the process or
+// falls back to the CPU: a shape no GPU kernel takes returns
+// BF_ERR_UNSUPPORTED.
+#include "bf_internal.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cstring>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+namespace bf {
+namespace {
+
+int to_status(cudaError_t e) {
+  if (e == cudaSuccess) return BF_OK;
+  if (e == cudaErrorMemoryAllocation) return BF_ERR_OUT_OF_MEMORY;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return BF_ERR_NO_DEVICE;
+  return BF_ERR_CUDA;
+}
+
+#define BF_TRY(expr)                          \
+  do {                                        \
+    const cudaError_t e_ = (expr);            \
+    if (e_ != cudaSuccess) return to_status(e_); \
+  } while (0)
+
+// Growable device buffer.
+struct DevBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+  cudaError_t reserve(size_t n) {
+    if (n <= cap) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    const cudaError_t e = cudaMalloc(&p, std::max<size_t>(n, 256));
+    if (e == cudaSuccess) cap = std::max<size_t>(n, 256);
+    return e;
+  }
+  template <class T>
+  T *as() const {
+    return static_cast<T *>(p);
+  }
+};
+
+struct DeviceCtx {
+  std::mutex mu;
+  bool ready = false;
+  int *err = nullptr;       // device error word written by kernels
+  uint32_t *adler = nullptr;  // device adler32 result
+  DevBuf E, A, G, J;        // staging for host-pointer calls
+  DevBuf W, bias;           // tensor-core operand for non-resident calls
+  DevBuf partials;          // adler32 partial sums
+};
+
+constexpr int kMaxDevices = 64;
+DeviceCtx g_ctx[kMaxDevices];
+
+int current_ctx(DeviceCtx **out) {
+  int dev = -1;
+  const cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return to_status(e);
+  if (dev < 0 || dev >= kMaxDevices) return BF_ERR_NO_DEVICE;
+  DeviceCtx &c = g_ctx[dev];
+  if (!c.ready) {
+    std::lock_guard<std::mutex> lk(c.mu);
+    if (!c.ready) {
+      BF_TRY(cudaMalloc(&c.err, sizeof(int)));
+      BF_TRY(cudaMemset(c.err, 0, sizeof(int)));
+      BF_TRY(cudaMalloc(&c.adler, sizeof(uint32_t)));
+      c.ready = true;
+    }
+  }
+  *out = &c;
+  return BF_OK;
+}
+
+std::mutex g_dims_mu;
+bool g_dims_set = false;
+bf_dims g_dims{};
+std::atomic<int> g_kernel{BF_KERNEL_AUTO};
+thread_local int t_last_status = BF_OK;
+thread_local const char *t_last_kernel = "none";
+
+bool dims_valid(const bf_dims *d) {
+  return d && d->ntimes >= 0 && d->nfrequencies >= 0 && d->ndishes >= 0 && d->npolarizations >= 0 &&
+         d->nbeams >= 0;
+}
+
+size_t esize(const bf_dims &d) {
+  return static_cast<size_t>(d.ntimes) * d.nfrequencies * d.ndishes * d.npolarizations;
+}
+size_t asize(const bf_dims &d) { return static_cast<size_t>(d.nfrequencies) * d.nbeams * d.ndishes; }
+size_t gsize(const bf_dims &d) { return static_cast<size_t>(d.nfrequencies) * d.nbeams; }
+size_t jsize(const bf_dims &d) {
+  return static_cast<size_t>(d.nbeams) * d.nfrequencies * d.npolarizations * d.ntimes;
+}
+
+// Sizes the operand layout for F x B x D weights.
+void plan_weights(TcWeights &w, int64_t F, int64_t B, int64_t D) {
+  w.F = F;
+  w.B = B;
+  w.D = D;
+  tc_plan_beams(B, &w.nb_pass, &w.npass);
+  w.nw = static_cast<int>((B + 7) / 8 * 8 * 2);
+  w.nw_pad = w.npass * 2 * w.nb_pass;
+}
+
+size_t weights_bytes(const TcWeights &w) { return static_cast<size_t>(w.F) * w.nw * 2 * w.D; }
+size_t bias_bytes(const TcWeights &w) { return static_cast<size_t>(w.F) * w.nw_pad * sizeof(float); }
+
+int choose_tensor(const bf_dims &d, bool *use_tc) {
+  const int k = g_kernel.load();
+  const bool ok = tc_supported(d);
+  if (k == BF_KERNEL_TENSOR && !ok) return BF_ERR_UNSUPPORTED;
+  if (k == BF_KERNEL_SIMT && (d.npolarizations < 1 || d.npolarizations > 2)) return BF_ERR_UNSUPPORTED;
+  if (k == BF_KERNEL_AUTO && !ok && (d.npolarizations < 1 || d.npolarizations > 2)) return BF_ERR_UNSUPPORTED;
+  *use_tc = (k == BF_KERNEL_TENSOR) || (k == BF_KERNEL_AUTO && ok);
+  return BF_OK;
+}
+
+// All four arrays on the device.  Operand scratch comes from ctx (caller holds ctx.mu).
+int run_device(DeviceCtx &c, const bf_dims &d, uint8_t *J, const uint8_t *E, const uint8_t *A, const float *G,
+               cudaStream_t s) {
+  if (jsize(d) == 0) return BF_OK;
+  bool use_tc = false;
+  const int st = choose_tensor(d, &use_tc);
+  if (st != BF_OK) return st;
+  if (use_tc && ((reinterpret_cast<uintptr_t>(E) | reinterpret_cast<uintptr_t>(J)) & 15u)) {
+    if (g_kernel.load() == BF_KERNEL_TENSOR) return BF_ERR_UNSUPPORTED;
+    use_tc = false;
+  }
+  if (!use_tc) {
+    t_last_kernel = "simt";
+    return to_status(launch_simt(d, J, E, A, G, s));
+  }
+  TcWeights w;
+  plan_weights(w, d.nfrequencies, d.nbeams, d.ndishes);
+  BF_TRY(c.W.reserve(weights_bytes(w)));
+  BF_TRY(c.bias.reserve(bias_bytes(w)));
+  w.W = c.W.as<uint8_t>();
+  w.bias = c.bias.as<float>();
+  w.G = G;
+  BF_TRY(launch_prep_weights(w, A, s));
+  t_last_kernel = "tensor";
+  return to_status(launch_tc(w, d.ntimes, J, E, c.err, s));
+}
+
+int read_and_clear_err(DeviceCtx &c, cudaStream_t s) {
+  int h = 0;
+  BF_TRY(cudaMemcpyAsync(&h, c.err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  BF_TRY(cudaStreamSynchronize(s));
+  if (h != 0) {
+    BF_TRY(cudaMemsetAsync(c.err, 0, sizeof(int), s));
+    BF_TRY(cudaStreamSynchronize(s));
+    return BF_ERR_DEVICE_TIMEOUT;
+  }
+  return BF_OK;
+}
+
+}  // namespace
+}  // namespace bf
+
+using namespace bf;
+
+struct bf_weights {
+  int device = 0;
+  TcWeights tc;
+  uint8_t *A = nullptr;  // raw A kept for the SIMT path
+  float *G = nullptr;
+};
+
+extern "C" {
+
+int bf_set_dims(const bf_dims *dims) {
+  if (!dims_valid(dims)) return BF_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(g_dims_mu);
+  g_dims = *dims;
+  g_dims_set = true;
+  return BF_OK;
+}
+
+int bf_last_status(void) { return t_last_status; }
+
+const char *bf_last_kernel(void) { return t_last_kernel; }
+
+const char *bf_status_string(int status) {
+  switch (status) {
+    case BF_OK: return "ok";
+    case BF_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case BF_ERR_UNSUPPORTED: return "shape or alignment not supported by any GPU kernel";
+    case BF_ERR_NO_DEVICE: return "no usable CUDA device";
+    case BF_ERR_CUDA: return "CUDA runtime error";
+    case BF_ERR_OUT_OF_MEMORY: return "out of memory";
+    case BF_ERR_DEVICE_TIMEOUT: return "a device-side wait expired; results are invalid";
+    case BF_ERR_NOT_CONFIGURED: return "form_beams() called before bf_set_dims()";
+    case BF_ERR_SIZE_MISMATCH: return "weights were built for a different shape";
+    default: return "unknown status";
+  }
+}
+
+int bf_set_kernel(int kernel) {
+  if (kernel < BF_KERNEL_AUTO || kernel > BF_KERNEL_SIMT) return BF_ERR_INVALID_ARGUMENT;
+  g_kernel.store(kernel);
+  return BF_OK;
+}
+
+int bf_set_test_stall(int on) {
+  tc_set_test_stall(on);
+  return BF_OK;
+}
+
+int bf_form_beams_ex(const bf_dims *dims, uint8_t *J, const uint8_t *E, const uint8_t *A, const float *G,
+                     int ptr_kind, bf_stream_t stream) {
+  if (!dims_valid(dims)) return BF_ERR_INVALID_ARGUMENT;
+  if (ptr_kind != BF_PTR_HOST && ptr_kind != BF_PTR_DEVICE) return BF_ERR_INVALID_ARGUMENT;
+  const bf_dims d = *dims;
+  if (jsize(d) == 0) return BF_OK;
+  if (!J || (esize(d) && !E) || (asize(d) && !A) || !G) return BF_ERR_INVALID_ARGUMENT;
+  DeviceCtx *c = nullptr;
+  int st = current_ctx(&c);
+  if (st != BF_OK) return st;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (ptr_kind == BF_PTR_DEVICE) return run_device(*c, d, J, E, A, G, s);
+
+  // Host pointers: stage in, compute, stage out, synchronously (cuda.cu:274-314 does the same around its kernel).
+  BF_TRY(c->E.reserve(esize(d)));
+  BF_TRY(c->A.reserve(asize(d)));
+  BF_TRY(c->G.reserve(gsize(d) * sizeof(float)));
+  BF_TRY(c->J.reserve(jsize(d)));
+  BF_TRY(cudaMemcpyAsync(c->E.p, E, esize(d), cudaMemcpyHostToDevice, s));
+  BF_TRY(cudaMemcpyAsync(c->A.p, A, asize(d), cudaMemcpyHostToDevice, s));
+  BF_TRY(cudaMemcpyAsync(c->G.p, G, gsize(d) * sizeof(float), cudaMemcpyHostToDevice, s));
+  st = run_device(*c, d, c->J.as<uint8_t>(), c->E.as<uint8_t>(), c->A.as<uint8_t>(), c->G.as<float>(), s);
+  if (st != BF_OK) return st;
+  BF_TRY(cudaMemcpyAsync(J, c->J.p, jsize(d), cudaMemcpyDeviceToHost, s));
+  return read_and_clear_err(*c, s);
+}
+
+void form_beams(uint8_t *J, const uint8_t *E, const uint8_t *A, const float *G) {
+  bf_dims d;
+  {
+    std::lock_guard<std::mutex> lk(g_dims_mu);
+    if (!g_dims_set) {
+      t_last_status = BF_ERR_NOT_CONFIGURED;
+      return;
+    }
+    d = g_dims;
+  }
+  t_last_status = bf_form_beams_ex(&d, J, E, A, G, BF_PTR_HOST, nullptr);
+}
+
+int bf_stream_status(bf_stream_t stream) {
+  DeviceCtx *c = nullptr;
+  const int st = current_ctx(&c);
+  if (st != BF_OK) return st;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const cudaError_t e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return to_status(e);
+  return read_and_clear_err(*c, s);
+}
+
+int bf_weights_create(bf_weights **out, int64_t nfrequencies, int64_t nbeams, int64_t ndishes, const uint8_t *A,
+                      const float *G, int ptr_kind, bf_stream_t stream) {
+  if (!out || nfrequencies <= 0 || nbeams <= 0 || ndishes <= 0 || !A || !G) return BF_ERR_INVALID_ARGUMENT;
+  if (ptr_kind != BF_PTR_HOST && ptr_kind != BF_PTR_DEVICE) return BF_ERR_INVALID_ARGUMENT;
+  DeviceCtx *c = nullptr;
+  int st = current_ctx(&c);
+  if (st != BF_OK) return st;
+  bf_weights *w = new bf_weights();
+  cudaGetDevice(&w->device);
+  plan_weights(w->tc, nfrequencies, nbeams, ndishes);
+  const size_t na = static_cast<size_t>(nfrequencies) * nbeams * ndishes;
+  const size_t ng = static_cast<size_t>(nfrequencies) * nbeams;
+  cudaError_t e = cudaMalloc(&w->A, na);
+  if (e == cudaSuccess) e = cudaMalloc(&w->G, ng * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&w->tc.W, weights_bytes(w->tc));
+  if (e == cudaSuccess) e = cudaMalloc(&w->tc.bias, bias_bytes(w->tc));
+  if (e != cudaSuccess) {
+    bf_weights_destroy(w);
+    return to_status(e);
+  }
+  w->tc.G = w->G;
+  st = bf_weights_update(w, A, G, ptr_kind, stream);
+  if (st != BF_OK) {
+    bf_weights_destroy(w);
+    return st;
+  }
+  *out = w;
+  return BF_OK;
+}
+
+int bf_weights_update(bf_weights *w, const uint8_t *A, const float *G, int ptr_kind, bf_stream_t stream) {
+  if (!w || !A || !G) return BF_ERR_INVALID_ARGUMENT;
+  if (ptr_kind != BF_PTR_HOST && ptr_kind != BF_PTR_DEVICE) return BF_ERR_INVALID_ARGUMENT;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const size_t na = static_cast<size_t>(w->tc.F) * w->tc.B * w->tc.D;
+  const size_t ng = static_cast<size_t>(w->tc.F) * w->tc.B;
+  const cudaMemcpyKind k = ptr_kind == BF_PTR_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+  BF_TRY(cudaMemcpyAsync(w->A, A, na, k, s));
+  BF_TRY(cudaMemcpyAsync(w->G, G, ng * sizeof(float), k, s));
+  BF_TRY(launch_prep_weights(w->tc, w->A, s));
+  if (ptr_kind == BF_PTR_HOST) BF_TRY(cudaStreamSynchronize(s));
+  return BF_OK;
+}
+
+int bf_weights_destroy(bf_weights *w) {
+  if (!w) return BF_OK;
+  if (w->A) cudaFree(w->A);
+  if (w->G) cudaFree(w->G);
+  if (w->tc.W) cudaFree(w->tc.W);
+  if (w->tc.bias) cudaFree(w->tc.bias);
+  delete w;
+  return BF_OK;
+}
+
+int bf_form_beams_resident(const bf_weights *w, int64_t ntimes, uint8_t *J, const uint8_t *E, bf_stream_t stream) {
+  if (!w || ntimes < 0 || (ntimes > 0 && (!J || !E))) return BF_ERR_INVALID_ARGUMENT;
+  if (ntimes == 0) return BF_OK;
+  DeviceCtx *c = nullptr;
+  const int st = current_ctx(&c);
+  if (st != BF_OK) return st;
+  const bf_dims d{ntimes, w->tc.F, w->tc.D, 2, w->tc.B};
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  bool use_tc = false;
+  const int cs = choose_tensor(d, &use_tc);
+  if (cs != BF_OK) return cs;
+  if (use_tc && ((reinterpret_cast<uintptr_t>(E) | reinterpret_cast<uintptr_t>(J)) & 15u)) {
+    if (g_kernel.load() == BF_KERNEL_TENSOR) return BF_ERR_UNSUPPORTED;
+    use_tc = false;
+  }
+  if (use_tc) {
+    t_last_kernel = "tensor";
+    return to_status(launch_tc(w->tc, ntimes, J, E, c->err, s));
+  }
+  t_last_kernel = "simt";
+  return to_status(launch_simt(d, J, E, w->A, w->G, s));
+}
+
+int bf_adler32_device(const uint8_t *data, size_t len, uint32_t *out, bf_stream_t stream) {
+  if (!out || (len && !data)) return BF_ERR_INVALID_ARGUMENT;
+  if (len == 0) {
+    *out = 1u;
+    return BF_OK;
+  }
+  DeviceCtx *c = nullptr;
+  const int st = current_ctx(&c);
+  if (st != BF_OK) return st;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  std::lock_guard<std::mutex> lk(c->mu);
+  BF_TRY(c->partials.reserve(static_cast<size_t>(adler_nchunks(len)) * 2 * sizeof(uint32_t)));
+  BF_TRY(launch_adler_partials(data, len, c->partials.as<uint32_t>(), s));
+  BF_TRY(launch_adler_combine(c->partials.as<uint32_t>(), len, c->adler, s));
+  uint32_t h = 0;
+  BF_TRY(cudaMemcpyAsync(&h, c->adler, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  BF_TRY(cudaStreamSynchronize(s));
+  *out = h;
+  return BF_OK;
+}
+
+int bf_fill_random_device(uint8_t *dst, size_t n, uint64_t seed, uint64_t stream_id, bf_stream_t stream) {
+  if (n && !dst) return BF_ERR_INVALID_ARGUMENT;
+  return to_status(launch_fill_random(dst, n, seed, stream_id, static_cast<cudaStream_t>(stream)));
+}
+
+int bf_fill_random_host(uint8_t *dst, size_t n, uint64_t seed, uint64_t stream_id) {
+  if (n && !dst) return BF_ERR_INVALID_ARGUMENT;
+  auto mix64 = [](uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+  };
+  const uint64_t key = mix64(seed * 2u + stream_id + 1u);
+  const size_t nwords = (n + 7) / 8;
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const size_t per = (nwords + hw - 1) / hw;
+  std::vector<std::thread> th;
+  for (unsigned i = 0; i < hw; ++i) {
+    const size_t j0 = i * per, j1 = std::min(nwords, j0 + per);
+    if (j0 >= j1) break;
+    th.emplace_back([=]() {
+      for (size_t j = j0; j < j1; ++j) {
+        const uint64_t w = mix64(key + static_cast<uint64_t>(j + 1) * 0x9E3779B97F4A7C15ull);
+        if (8 * j + 8 <= n) {
+          uint8_t b[8];
+          for (int k = 0; k < 8; ++k) b[k] = static_cast<uint8_t>(w >> (8 * k));
+          std::memcpy(dst + 8 * j, b, 8);
+        } else {
+          for (size_t k = 0; 8 * j + k < n; ++k) dst[8 * j + k] = static_cast<uint8_t>(w >> (8 * k));
+        }
+      }
+    });
+  }
+  for (auto &t : th) t.join();
+  return BF_OK;
+}
+
+int bf_gains_host(const bf_dims *dims, float *G) {
+  if (!dims_valid(dims) || !G) return BF_ERR_INVALID_ARGUMENT;
+  // arraysizes.cxx:31-32: float(n) / Gsize / ndishes * (15 + n % 15) / 30, left to right in float
+  const int64_t gs = dims->nfrequencies * dims->nbeams;
+  const float fg = static_cast<float>(static_cast<uint64_t>(gs));
+  const float fd = static_cast<float>(static_cast<uint64_t>(dims->ndishes));
+  for (int64_t n = 0; n < gs; ++n) {
+    float g = static_cast<float>(static_cast<uint64_t>(n));
+    g = g / fg;
+    g = g / fd;
+    g = g * static_cast<float>(static_cast<uint64_t>(15 + n % 15));
+    g = g / 30.0f;
+    G[n] = g;
+  }
+  return BF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,404 @@
+#!/usr/bin/env python3
+"""Throughput of the GB300 beamformer on the full single-GPU chunk.
+
+Workload: t=32768, f=84, d=512, p=2, b=96 (E = 2.82 GB), seeded inputs (seed
+1: E and A uniform bytes, G from the reference setup()'s gain formula).  One
+step is one form_beams pass over that chunk.  Metric: complex beam-MACs per
+second (one A[f,b,d] * E[t,f,d,p] complex multiply-add; t*f*p*b*d per pass).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`value` times K passes with inputs resident in HBM (inputs are larger than the
+129 MB L2, so no flush is needed); `e2e` times the same pass through the C-ABI
+host-pointer call, copies in and out included.  `--impl reference` times the
+reference's CPU algorithm (the oracle restatement of cpu.cxx) on the host
+cores.  Under torchrun every rank runs its own chunk (frequencies are
+independent; no collective), so scaling is weak.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = {"ntimes": 32768, "nfrequencies": 84, "ndishes": 512, "npolarizations": 2, "nbeams": 96, "seed": 1}
+WORKLOAD_NAME = "full single-GPU chunk t=32768 f=84 d=512 p=2 b=96 seed=1"
+METRIC = "complex beam-MACs/s"
+UNIT = "CMAC/s"
+PROFILE_SUMMARY = os.path.join(ROOT, "profiles", "form_beams_tc_full_chunk.md")
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU-baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dims():
+    import beamforming_gb300 as bf
+
+    w = WORKLOAD
+    return bf.Dims(w["ntimes"], w["nfrequencies"], w["ndishes"], w["npolarizations"], w["nbeams"])
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fp:
+            p = json.load(fp)
+        return float(p["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per launch of the tensor-core kernel from the committed ncu summary."""
+    if not os.path.exists(PROFILE_SUMMARY):
+        return None
+    for line in open(PROFILE_SUMMARY):
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return int(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) while the GPU is under load."""
+
+    FIELDS = (
+        "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+        "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+        "clocks_event_reasons.sw_power_cap"
+    )
+
+    def __init__(self, gpu_id: str | None):
+        self.gpu_id = gpu_id
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"]
+        if self.gpu_id:
+            cmd += ["-i", self.gpu_id]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=self.file, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.file.flush()
+        rows = []
+        with open(self.file.name) as fp:
+            for line in fp:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 8:
+                    rows.append(parts)
+        os.unlink(self.file.name)
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        smax = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[4 + i].lower() == "active"})
+        return {
+            "sm_mhz": statistics.median(sm) if sm else None,
+            "sm_max_mhz": max(smax) if smax else None,
+            "reasons": reasons,
+            "samples": len(rows),
+        }
+
+
+def cpu_baseline(target_s: float):
+    """The oracle (the reference's cpu.cxx restated) on a sample of frequencies of the workload."""
+    import beamforming_gb300 as bf
+    from oracle import oracle as O
+
+    d = dims()
+    E = np.empty(d.esize, np.uint8)
+    bf.fill_random_host(E, WORKLOAD["seed"], 0)
+    A = np.empty(d.asize, np.uint8)
+    bf.fill_random_host(A, WORKLOAD["seed"], 1)
+    G = bf.gains(d)
+    E4 = E.reshape(d.ntimes, d.nfrequencies, -1)
+    A2 = A.reshape(d.nfrequencies, -1)
+    G2 = G.reshape(d.nfrequencies, -1)
+
+    def run(nf):
+        sub = O.Dims(d.ntimes, nf, d.ndishes, 2, d.nbeams)
+        Es = np.ascontiguousarray(E4[:, :nf]).reshape(-1)
+        As = np.ascontiguousarray(A2[:nf]).reshape(-1)
+        Gs = np.ascontiguousarray(G2[:nf]).reshape(-1)
+        t0 = time.perf_counter()
+        O.form_beams(sub, Es, As, Gs)
+        return time.perf_counter() - t0, sub.cmacs
+
+    t1, _ = run(1)
+    nf = int(max(1, min(d.nfrequencies, round(target_s / max(t1, 1e-3)))))
+    t, cm = run(nf)
+    cores = os.cpu_count() or 1
+    return {
+        "value": cm / t,
+        "unit": UNIT,
+        "cores": cores,
+        "kind": "port",
+        "sample": f"{nf} of {d.nfrequencies} frequencies of the workload ({cm:.3e} CMAC, {t:.2f} s, "
+        f"OpenMP threads = {cores})",
+    }
+
+
+def run_reference(args):
+    """Reference arm: the reference's CPU algorithm on the host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import beamforming_gb300 as bf  # noqa: F401  (workload generator)
+    from oracle import oracle as O
+
+    d = dims()
+    nf = 1  # one frequency of the chunk per step
+    sub = O.Dims(d.ntimes, nf, d.ndishes, 2, d.nbeams)
+    E = np.empty(d.esize, np.uint8)
+    bf.fill_random_host(E, WORKLOAD["seed"], 0)
+    A = np.empty(d.asize, np.uint8)
+    bf.fill_random_host(A, WORKLOAD["seed"], 1)
+    G = bf.gains(d)
+    E4 = E.reshape(d.ntimes, d.nfrequencies, -1)
+    samples = []
+    for i in range(args.warmup + args.steps):
+        f = i % d.nfrequencies
+        Es = np.ascontiguousarray(E4[:, f]).reshape(-1)
+        As = np.ascontiguousarray(A.reshape(d.nfrequencies, -1)[f])
+        Gs = np.ascontiguousarray(G.reshape(d.nfrequencies, -1)[f])
+        t0 = time.perf_counter()
+        O.form_beams(sub, Es, As, Gs)
+        if i >= args.warmup:
+            samples.append(time.perf_counter() - t0)
+    total = sum(samples)
+    value = sub.cmacs * len(samples) / total
+    cores = os.cpu_count() or 1
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / len(samples),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "int4 complex in, int32 sums",
+        "data": "synthetic (seeded uniform 4-bit complex)",
+        "config": {"workload": WORKLOAD_NAME, **WORKLOAD, "sample_per_step": "one frequency (t=32768, d=512, b=96)"},
+        "cpu_baseline": {
+            "value": value,
+            "unit": UNIT,
+            "cores": cores,
+            "kind": "port",
+            "sample": "one frequency of the chunk per step; oracle restatement of cpu.cxx:15-46 with OpenMP",
+        },
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+
+    import beamforming_gb300 as bf
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    d = dims()
+    seed = WORKLOAD["seed"]
+    E = torch.empty(d.esize, dtype=torch.uint8, device="cuda")
+    A = torch.empty(d.asize, dtype=torch.uint8, device="cuda")
+    bf.fill_random_device(E, seed, 0)
+    bf.fill_random_device(A, seed, 1)
+    G = torch.from_numpy(bf.gains(d)).cuda()
+    J = torch.empty(d.jsize, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    for _ in range(max(3, args.warmup)):
+        bf.form_beams_ex(d, J, E, A, G, stream=stream)
+    bf.stream_status(stream)
+    checksum = bf.adler32_device(J)
+
+    gpu_id = None
+    try:
+        gpu_id = "GPU-" + str(torch.cuda.get_device_properties(local_rank).uuid)
+    except Exception:
+        gpu_id = None
+    clocks = ClockSampler(gpu_id if rank == 0 else None)
+    if rank == 0:
+        clocks.start()
+    # keep the GPU busy ~1 s before the timed region so the clock samples cover the load
+    t_end = time.perf_counter() + 1.0
+    while time.perf_counter() < t_end:
+        for _ in range(20):
+            bf.form_beams_ex(d, J, E, A, G, stream=stream)
+        torch.cuda.synchronize()
+
+    barrier()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        bf.form_beams_ex(d, J, E, A, G, stream=stream)
+    ev1.record(stream)
+    barrier()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    clk = clocks.stop() if rank == 0 else None
+    bf.stream_status(stream)
+    ms_t = torch.tensor([ms], device="cuda")
+    if dist is not None:
+        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
+    ms_max = float(ms_t.item())
+    value = d.cmacs * world / (ms_max * 1e-3)
+
+    # dominant kernel alone: resident weights, one tensor-core launch per event pair
+    W = bf.ResidentWeights(d.nfrequencies, d.nbeams, d.ndishes, A, G, stream=stream)
+    for _ in range(3):
+        W.form_beams(J, E, d.ntimes, stream=stream)
+    torch.cuda.synchronize()
+    n_k = max(10, min(args.steps, 200))
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n_k)]
+    for a, b in evs:
+        a.record(stream)
+        W.form_beams(J, E, d.ntimes, stream=stream)
+        b.record(stream)
+    torch.cuda.synchronize()
+    bf.stream_status(stream)
+    k_ms = statistics.mean(a.elapsed_time(b) for a, b in evs)
+    assert bf.adler32_device(J) == checksum
+    W.close()
+    alg_bytes = d.esize + d.jsize + d.asize + 4 * d.gsize
+    peak, peak_kind = load_peaks()
+    achieved = alg_bytes / (k_ms * 1e-3) / 1e9
+    roofline = {
+        "bound": "hbm",
+        "kernel": "bf_form_beams_tc",
+        "achieved": round(achieved, 1),
+        "peak": peak,
+        "peak_kind": f"{peak_kind} (copy bandwidth)",
+        "unit": "GB/s",
+        "frac": round(achieved / peak, 4),
+        "traffic": profile_traffic(),
+        "algorithmic_bytes": alg_bytes,
+        "kernel_ms": round(k_ms, 4),
+        "tensor_fp8_tflops": round(8 * d.cmacs / (k_ms * 1e-3) / 1e12, 1),
+    }
+
+    e2e = None
+    if not args.no_e2e:
+        Eh = torch.empty(d.esize, dtype=torch.uint8, pin_memory=True)
+        Ah = torch.empty(d.asize, dtype=torch.uint8, pin_memory=True)
+        Gh = torch.empty(d.gsize, dtype=torch.float32, pin_memory=True)
+        Jh = torch.empty(d.jsize, dtype=torch.uint8, pin_memory=True)
+        Eh.copy_(E)
+        Ah.copy_(A)
+        Gh.copy_(G)
+        En, An, Gn, Jn = Eh.numpy(), Ah.numpy(), Gh.numpy(), Jh.numpy()
+        bf.form_beams_ex(d, Jn, En, An, Gn)  # warm the staging buffers
+        n_e = max(3, min(args.steps, 20))
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(n_e):
+            bf.form_beams_ex(d, Jn, En, An, Gn)
+        barrier()
+        e_s = (time.perf_counter() - t0) / n_e
+        import zlib
+
+        assert zlib.adler32(Jn.tobytes()) == checksum
+        e2e = {
+            "value": d.cmacs * world / e_s,
+            "unit": UNIT,
+            "ms_per_step": round(1e3 * e_s, 3),
+            "h2d_bytes_per_step": d.esize + d.asize + 4 * d.gsize,
+            "d2h_bytes_per_step": d.jsize,
+            "api": "bf_form_beams_ex(ptr_kind=BF_PTR_HOST), pinned host buffers",
+        }
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(args.cpu_seconds)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC,
+            "value": value,
+            "unit": UNIT,
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": round(ms_max, 4),
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "int4 complex in, exact integer sums (e4m3 tensor-core operands, f32 accumulate)",
+            "data": "synthetic (seeded uniform 4-bit complex; G from the reference setup() formula)",
+            "config": {
+                "workload": WORKLOAD_NAME,
+                **WORKLOAD,
+                "parallelism": f"replicas x{world} (frequencies independent, no collective)",
+                "l2": "inputs larger than L2 (E = 2.82 GB), no flush",
+                "adler32_J": f"0x{checksum:08x}",
+            },
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "clocks": clk,
+            "gpu_launches": 2 * args.steps,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

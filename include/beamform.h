@@ -1,0 +1,164 @@
+/*
+ * beamform.h -- C ABI of the GB300 (sm_103a) CHORD beamformer.
+ *
+ * Computes, for every beam b, frequency f, polarization p and time t,
+ *
+ *   J[b][f][p][t] = ucomplex4(clamp(lrint(G[f][b] * float(re)), -7, 7),
+ *                             clamp(lrint(G[f][b] * float(im)), -7, 7))
+ *   re + i*im    = sum_d A[f][b][d] * E[t][f][d][p]        (exact integers)
+ *
+ * over 4-bit complex data stored as ucomplex4 bytes (real part in the high
+ * nibble, imaginary part in the low nibble, each stored as value + 8).  The
+ * result is bit-identical to the reference CPU implementation
+ * (eschnett/beamforming cpu.cxx:15-46).
+ *
+ * Array layouts (all byte arrays, C order) follow the reference accessors:
+ *   E[t][f][d][p]   Elinear   arraysizes.hxx:80
+ *   A[f][b][d]      Alinear   arraysizes.hxx:115
+ *   G[f][b] float   Glinear   arraysizes.hxx:136
+ *   J[b][f][p][t]   Jlinear   arraysizes.hxx:92
+ *
+ * Every entry point except form_beams() returns a bf_status; none of them
+ * exits the process.
+ */
+#ifndef BEAMFORM_H
+#define BEAMFORM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define BF_API __attribute__((visibility("default")))
+#else
+#define BF_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Problem shape: the reference's compile-time sizes (arraysizes.hxx:22-27)
+ * made run-time values. */
+typedef struct bf_dims {
+  int64_t ntimes;
+  int64_t nfrequencies;
+  int64_t ndishes;
+  int64_t npolarizations;
+  int64_t nbeams;
+} bf_dims;
+
+/* A CUDA stream (cudaStream_t); NULL means the legacy default stream. */
+typedef void *bf_stream_t;
+
+typedef enum bf_status {
+  BF_OK = 0,
+  BF_ERR_INVALID_ARGUMENT = 1, /* null pointer, negative size, bad enum */
+  BF_ERR_UNSUPPORTED = 2,      /* shape or alignment no kernel handles */
+  BF_ERR_NO_DEVICE = 3,        /* no CUDA device, or not a compute-capability 10.3 part */
+  BF_ERR_CUDA = 4,             /* a CUDA runtime call failed */
+  BF_ERR_OUT_OF_MEMORY = 5,    /* device or pinned-host allocation failed */
+  BF_ERR_DEVICE_TIMEOUT = 6,   /* a kernel's bounded wait expired; the result is invalid */
+  BF_ERR_NOT_CONFIGURED = 7,   /* form_beams() called before bf_set_dims() */
+  BF_ERR_SIZE_MISMATCH = 8     /* resident weights built for another shape */
+} bf_status;
+
+/* Where the array arguments live. */
+typedef enum bf_ptr_kind { BF_PTR_HOST = 0, BF_PTR_DEVICE = 1 } bf_ptr_kind;
+
+/* Which kernel family runs the beam sums. */
+typedef enum bf_kernel {
+  BF_KERNEL_AUTO = 0,   /* tensor-core kernel where the shape allows, else SIMT */
+  BF_KERNEL_TENSOR = 1, /* tcgen05 tensor-core kernel (fails if the shape does not fit) */
+  BF_KERNEL_SIMT = 2    /* exact integer dp4a kernel, any shape */
+} bf_kernel;
+
+/* ------------------------------------------------------------------ drop-in */
+
+/* Sets the sizes form_beams() uses.  Replaces the constexpr globals of
+ * arraysizes.hxx:22-27. */
+BF_API int bf_set_dims(const bf_dims *dims);
+
+/* Drop-in for the reference's
+ *   void form_beams(ucomplex4 *J, const ucomplex4 *E, const ucomplex4 *A, const float *G)
+ * (cpu.cxx:15-16): host pointers, sizes from bf_set_dims(), synchronous, no
+ * return value.  J must hold Jsize/2 bytes.  The status of the last call is
+ * available from bf_last_status(). */
+BF_API void form_beams(uint8_t *J, const uint8_t *E, const uint8_t *A, const float *G);
+
+/* Status of the most recent form_beams() call on this thread. */
+BF_API int bf_last_status(void);
+
+/* Human-readable text for a status code (static storage). */
+BF_API const char *bf_status_string(int status);
+
+/* -------------------------------------------------------------- explicit API */
+
+/* One beamforming pass with explicit sizes.  ptr_kind says whether E, A, G and
+ * J are host or device pointers.  Device pointers: asynchronous on `stream`;
+ * call bf_stream_status() (or synchronize) before reading J.  Host pointers:
+ * synchronous (copies in, computes, copies out). */
+BF_API int bf_form_beams_ex(const bf_dims *dims, uint8_t *J, const uint8_t *E, const uint8_t *A, const float *G,
+                     int ptr_kind, bf_stream_t stream);
+
+/* Synchronizes `stream` and reports any CUDA error or expired device wait
+ * recorded by kernels launched by this library since the last call. */
+BF_API int bf_stream_status(bf_stream_t stream);
+
+/* Chooses the kernel family for later calls (testing and benchmarking). */
+BF_API int bf_set_kernel(int kernel);
+
+/* Test hook for the failure path: while `on` is nonzero, tensor-core launches
+ * issue no input copies, so their bounded device waits expire (after about
+ * 1.5 s) and the call reports BF_ERR_DEVICE_TIMEOUT.  No memory is touched
+ * out of bounds and the CUDA context stays usable. */
+BF_API int bf_set_test_stall(int on);
+
+/* Name of the kernel family the last launch on this thread used:
+ * "tensor", "simt" or "none". */
+BF_API const char *bf_last_kernel(void);
+
+/* --------------------------------------------------------- resident weights */
+
+/* Beam weights kept on the device in the tensor-core operand format, so a
+ * stream of voltage chunks for the same frequencies does not re-prepare A. */
+typedef struct bf_weights bf_weights;
+
+/* Allocates device storage for the weights of nfrequencies x nbeams x ndishes
+ * (2 polarizations) and fills it from A and G (ptr_kind as above). */
+BF_API int bf_weights_create(bf_weights **out, int64_t nfrequencies, int64_t nbeams, int64_t ndishes, const uint8_t *A,
+                      const float *G, int ptr_kind, bf_stream_t stream);
+
+/* Replaces the weights in place (same sizes): weight refresh. */
+BF_API int bf_weights_update(bf_weights *w, const uint8_t *A, const float *G, int ptr_kind, bf_stream_t stream);
+
+BF_API int bf_weights_destroy(bf_weights *w);
+
+/* Beamforms ntimes samples of device-resident E into device J with resident
+ * weights; asynchronous on `stream`. */
+BF_API int bf_form_beams_resident(const bf_weights *w, int64_t ntimes, uint8_t *J, const uint8_t *E, bf_stream_t stream);
+
+/* ---------------------------------------------------------------- checksum */
+
+/* adler32 (adler32.c:7-20) of `len` bytes of device memory; the result is
+ * written to *out (host).  Synchronous on `stream`. */
+BF_API int bf_adler32_device(const uint8_t *data, size_t len, uint32_t *out, bf_stream_t stream);
+
+/* ------------------------------------------------------- workload generator */
+
+/* Seeded uniform bytes (each ucomplex4 nibble uniform on [-8,7]) into device
+ * memory: byte i is byte (i % 8), little-endian, of
+ *   mix64(key + (i/8 + 1) * 0x9E3779B97F4A7C15),  key = mix64(seed * 2 + stream_id + 1),
+ * mix64 the SplitMix64 finaliser.  stream_id 0 is used for E, 1 for A. */
+BF_API int bf_fill_random_device(uint8_t *dst, size_t n, uint64_t seed, uint64_t stream_id, bf_stream_t stream);
+
+/* The same bytes into host memory (multi-threaded). */
+BF_API int bf_fill_random_host(uint8_t *dst, size_t n, uint64_t seed, uint64_t stream_id);
+
+/* setup()'s gain formula (arraysizes.cxx:31-32) for a shape, into host memory. */
+BF_API int bf_gains_host(const bf_dims *dims, float *G);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BEAMFORM_H */
