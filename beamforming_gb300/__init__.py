@@ -31,6 +31,7 @@ ERR_OUT_OF_MEMORY = 5
 ERR_DEVICE_TIMEOUT = 6
 ERR_NOT_CONFIGURED = 7
 ERR_SIZE_MISMATCH = 8
+ERR_TOO_LARGE = 9
 
 PTR_HOST = 0
 PTR_DEVICE = 1
@@ -52,6 +53,7 @@ EXPORTED_SYMBOLS = (
     "bf_weights_update",
     "bf_weights_destroy",
     "bf_form_beams_resident",
+    "bf_form_beams_noalloc",
     "bf_adler32_device",
     "bf_fill_random_device",
     "bf_fill_random_host",
@@ -151,6 +153,7 @@ def lib() -> ctypes.CDLL:
         L.bf_weights_update.argtypes = [vp, u8p, fp, ctypes.c_int, vp]
         L.bf_weights_destroy.argtypes = [vp]
         L.bf_form_beams_resident.argtypes = [vp, ctypes.c_int64, u8p, u8p, vp]
+        L.bf_form_beams_noalloc.argtypes = [D, u8p, u8p, u8p, fp, vp]
         L.bf_adler32_device.argtypes = [u8p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_uint32), vp]
         L.bf_fill_random_device.argtypes = [u8p, ctypes.c_size_t, ctypes.c_uint64, ctypes.c_uint64, vp]
         L.bf_fill_random_host.argtypes = [u8p, ctypes.c_size_t, ctypes.c_uint64, ctypes.c_uint64]

@@ -201,6 +201,7 @@ const char *bf_status_string(int status) {
     case BF_ERR_DEVICE_TIMEOUT: return "a device-side wait expired; results are invalid";
     case BF_ERR_NOT_CONFIGURED: return "form_beams() called before bf_set_dims()";
     case BF_ERR_SIZE_MISMATCH: return "weights were built for a different shape";
+    case BF_ERR_TOO_LARGE: return "problem exceeds the fixed scratch of bf_form_beams_noalloc";
     default: return "unknown status";
   }
 }

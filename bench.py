@@ -47,6 +47,12 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument(
+        "--profile-kernel",
+        action="store_true",
+        help="only launch the tensor-core kernel (resident weights), for ncu captures; prints no measurement",
+    )
+    ap.add_argument("--frequencies", type=int, default=None, help="override f (profiling a smaller case)")
     return ap.parse_args()
 
 
@@ -392,9 +398,36 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def profile_kernel(args):
+    """Tensor-core kernel launches only (resident weights), nothing timed."""
+    import torch
+
+    import beamforming_gb300 as bf
+
+    d = dims()
+    torch.cuda.set_device(0)
+    E = torch.empty(d.esize, dtype=torch.uint8, device="cuda")
+    A = torch.empty(d.asize, dtype=torch.uint8, device="cuda")
+    bf.fill_random_device(E, WORKLOAD["seed"], 0)
+    bf.fill_random_device(A, WORKLOAD["seed"], 1)
+    G = torch.from_numpy(bf.gains(d)).cuda()
+    J = torch.empty(d.jsize, dtype=torch.uint8, device="cuda")
+    W = bf.ResidentWeights(d.nfrequencies, d.nbeams, d.ndishes, A, G)
+    for _ in range(args.warmup + args.steps):
+        W.form_beams(J, E, d.ntimes)
+    bf.stream_status()
+    print(json.dumps({"profile_kernel": True, "dims": d.__dict__, "adler32_J": hex(bf.adler32_device(J))}))
+
+
 def main():
     args = parse_args()
-    if args.impl == "reference":
+    if args.frequencies:
+        WORKLOAD["nfrequencies"] = args.frequencies
+        global WORKLOAD_NAME
+        WORKLOAD_NAME = WORKLOAD_NAME.replace("f=84", f"f={args.frequencies}")
+    if args.profile_kernel:
+        profile_kernel(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

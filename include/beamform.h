@@ -59,7 +59,8 @@ typedef enum bf_status {
   BF_ERR_OUT_OF_MEMORY = 5,    /* device or pinned-host allocation failed */
   BF_ERR_DEVICE_TIMEOUT = 6,   /* a kernel's bounded wait expired; the result is invalid */
   BF_ERR_NOT_CONFIGURED = 7,   /* form_beams() called before bf_set_dims() */
-  BF_ERR_SIZE_MISMATCH = 8     /* resident weights built for another shape */
+  BF_ERR_SIZE_MISMATCH = 8,    /* resident weights built for another shape */
+  BF_ERR_TOO_LARGE = 9         /* problem exceeds bf_form_beams_noalloc()'s fixed scratch */
 } bf_status;
 
 /* Where the array arguments live. */
@@ -136,6 +137,30 @@ BF_API int bf_weights_destroy(bf_weights *w);
 /* Beamforms ntimes samples of device-resident E into device J with resident
  * weights; asynchronous on `stream`. */
 BF_API int bf_form_beams_resident(const bf_weights *w, int64_t ntimes, uint8_t *J, const uint8_t *E, bf_stream_t stream);
+
+/* ------------------------------------------------------- no allocation */
+
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory -- e.g. a real-time pipeline that sizes all device memory once at
+ * start-up and must not allocate mid-stream, or a host framework that owns
+ * the memory pool: the tensor-core pass of bf_form_beams_ex(..., BF_PTR_DEVICE,
+ * ...) with its scratch (prepared weight operand, row sums, error word) in one
+ * fixed 4 MiB device array that every GPU loading the library holds until the
+ * process exits.  It calls no cudaMalloc, cudaFree or other allocating routine.
+ *
+ * E, A, G and J are device pointers.  Limits: the tensor-core shape rules
+ * (npolarizations == 2, ndishes % 8 == 0, ntimes % 16 == 0, E and J 16-byte
+ * aligned; else BF_ERR_UNSUPPORTED) and
+ *   256 + roundup256(4 * F * npass * 2 * nb) + F * 2 * roundup(B, 8) * 2 * D <= 4 MiB
+ * (nb = min(roundup(B, 8), 128), npass = ceil(roundup(B, 8) / nb); else
+ * BF_ERR_TOO_LARGE) -- e.g. f=16, b=96, d=512 fits, f=84 does not.
+ * Synchronous: returns once the pass on `stream` has finished, with its status.
+ * The first call on a device looks up the array's device address; make that
+ * first call before any stream capture.  All calls on a device share the one
+ * array and each call overwrites it: calls that overlap on the GPU (e.g. from
+ * two host threads at once) race and must be serialised by the caller. */
+BF_API int bf_form_beams_noalloc(const bf_dims *dims, uint8_t *J, const uint8_t *E, const uint8_t *A,
+                                 const float *G, bf_stream_t stream);
 
 /* ---------------------------------------------------------------- checksum */
 
