@@ -45,6 +45,10 @@ cudaError_t launch_tc(const TcWeights &w, int64_t T, uint8_t *J, const uint8_t *
 // launches issue nothing, so the kernel's bounded waits expire.
 void tc_set_test_stall(int on);
 
+// Shared-memory ring depths of the tensor-core kernel (0 = planner default):
+// W slots and raw E slots.
+void tc_set_ring_plan(int wslots, int raw);
+
 // Checksum ----------------------------------------------------------------------
 // Partial adler sums over chunks; `partials` holds 2 * nchunks uint32.
 int adler_nchunks(size_t len);

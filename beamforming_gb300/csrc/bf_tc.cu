@@ -2,8 +2,8 @@
 //
 // The complex sum of cpu.cxx:26-35 becomes one real GEMM per frequency:
 //
-//   rows    m = (p, t)      128 per tile: 64 times x 2 polarizations
-//   columns n = (b, re|im)  2 * beams (<= 256 per pass)
+//   rows    m = (t, p)      128 per tile: 64 times x 2 polarizations
+//   columns n = (b, re|im)  2 * beams (<= 192 per pass)
 //   depth   k = (d, re|im)  2 * dishes
 //
 //   [Jre]   [ Ar  -Ai ] [Ere]
@@ -23,11 +23,19 @@
 // requantisation clamp(lrint(G * float(raw)), -7, 7) of cpu.cxx:37-39 runs in
 // the epilogue with one IEEE multiply and a round-half-even conversion.
 //
-// Warp roles (one CTA per SM, persistent over tiles):
-//   warps 0-3  epilogue: TMEM -> registers -> requantise -> J tile in smem -> TMA store
-//   warp  4    TMA producer: raw E tile and the W slice of each K stage
-//   warp  5    TMEM allocator and single-thread MMA issuer
-//   warps 6-9  unpack: raw E bytes -> de-interleaved E4M3 operand (128B-swizzled)
+// Warp roles (one 608-thread CTA per SM, persistent over tiles):
+//   warps 0-7    epilogue: TMEM accumulator -> registers -> requantise -> 4x4 byte
+//                transpose across lanes -> 32-bit stores of 4 consecutive times of one beam
+//   warp  8      E producer: TMA of raw E boxes into a deep ring released by the unpack
+//   warp  9      TMEM allocator and single-thread MMA issuer (A operand from TMEM)
+//   warp  10     W producer: TMA of the W slice of each K stage, released by the MMA
+//   warps 11-18  unpack, two groups of four taking alternate K stages: raw E bytes ->
+//                de-interleaved E4M3 operand rows written straight into tensor memory
+//                (tcgen05.st); no shared-memory operand
+//
+// GEMM row r of a tile (TMEM lane r) is (t, p) = (r / 2, r % 2) for the 64 times
+// of the tile.  TMEM columns: accumulators at [0, N) and [256, 256 + N), unpacked
+// E stages (32 columns = 128 K bytes each) in the remaining columns.
 #include "bf_internal.h"
 #include "bf_ptx.cuh"
 
@@ -38,53 +46,78 @@
 namespace bf {
 namespace {
 
-constexpr int kThreads = 320;
-constexpr int kTmaWarp = 4;
-constexpr int kMmaWarp = 5;
-constexpr int kUnpackWarp0 = 6;
+constexpr int kThreads = 608;
+constexpr int kEpiThreads = 256;        // warps 0-7
+constexpr int kEProdWarp = 8;
+constexpr int kMmaWarp = 9;
+constexpr int kWProdWarp = 10;
+constexpr int kUnpackWarp0 = 11;        // warps 11-18: two groups, each covering TMEM lane quarters 3, 0, 1, 2
 constexpr int kTT = 64;                 // times per tile
 constexpr int kBM = 128;                // GEMM rows per tile
 constexpr int kKC = 128;                // K bytes per stage (64 dishes x re/im)
 constexpr int kRawBytes = kTT * kKC;    // raw E per stage: 64 times x 64 dishes x 2 pol
-constexpr int kABytes = kBM * kKC;      // unpacked operand per stage
-constexpr int kAccCols = 256;           // TMEM columns per accumulator buffer
+constexpr int kAccCols = 256;           // TMEM column offset of the second accumulator
+constexpr int kStageCols = kKC / 4;     // TMEM columns per unpacked stage
 constexpr int kSmemLimit = 232448;      // 227 KiB opt-in per block
-constexpr int kMaxStages = 6;
+constexpr int kMaxStages = 8;
+constexpr int kMaxWSlots = 6;
+constexpr int kMinRaw = 8;
+constexpr int kMaxRaw = 16;
 
 struct TcParams {
   int T, F, D, B;
+  uint8_t *J;
   int nb_pass;  // beams per pass
   int npass;
   int ntt;      // time tiles per frequency
   int nk;       // K stages per tile
   int ntiles;
-  int stages;
+  int stages;   // unpacked-operand stages in TMEM
+  int wslots;   // W slots in smem
+  int raw;      // raw E slots in smem
   int nw_pad;
-  int test_stall;  // nonzero: the producer issues nothing (failure-path test)
+  int test_stall;  // nonzero: the producers issue nothing (failure-path test)
   const float *G;
   const float *bias;
   int *err;
 };
 
 struct SmemPlan {
-  int stages, wbytes, jbytes;
-  int off_a, off_w, off_r, off_j, off_bar, total;
+  int wbytes;
+  int off_w, off_r, off_g, off_bar, nbar, total;
 };
 
-__host__ __device__ inline SmemPlan smem_plan(int stages, int nb_pass) {
+__host__ __device__ inline SmemPlan smem_plan(int stages, int wslots, int raw, int nb_pass) {
   SmemPlan s{};
-  s.stages = stages;
   s.wbytes = 2 * nb_pass * kKC;
-  s.jbytes = nb_pass * 2 * kTT;
-  s.off_a = 0;
-  s.off_w = s.off_a + stages * kABytes;
-  s.off_r = s.off_w + stages * s.wbytes;
-  s.off_j = s.off_r + stages * kRawBytes;
-  s.off_bar = s.off_j + 2 * s.jbytes;
-  // full[S], afull[S], empty[S], accfull[2], accempty[2], tmem address
-  s.total = s.off_bar + 8 * (3 * stages + 4) + 16;
+  s.off_w = 0;
+  s.off_r = s.off_w + wslots * s.wbytes;
+  // two buffers of gains [nb_pass] + row sums [2 * nb_pass]: this tile's and the next tile's
+  s.off_g = s.off_r + raw * kRawBytes;
+  s.off_bar = s.off_g + 2 * 3 * nb_pass * 4;
+  // raw_full[R], raw_empty[R], w_full[SW], w_empty[SW], a_full[S], empty[S], accfull[2], accempty[2]
+  s.nbar = 2 * raw + 2 * wslots + 2 * stages + 4;
+  s.total = s.off_bar + 8 * s.nbar + 16;
   return s;
 }
+
+// TMEM column of unpacked stage i: the columns left over after the two accumulators.
+__host__ __device__ inline uint32_t stage_col(int i, int ncols, int per_half) {
+  return i < per_half ? static_cast<uint32_t>(ncols + kStageCols * i)
+                      : static_cast<uint32_t>(kAccCols + ncols + kStageCols * (i - per_half));
+}
+
+// Position in a ring of n slots: slot index and the parity of the pass over the ring.
+struct Ring {
+  uint32_t idx = 0, phase = 0, n;
+  __device__ explicit Ring(int n_) : n(static_cast<uint32_t>(n_)) {}
+  __device__ __forceinline__ void advance() {
+    if (++idx == n) {
+      idx = 0;
+      phase ^= 1u;
+    }
+  }
+};
 
 __device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel) {
   uint32_t r;
@@ -92,42 +125,53 @@ __device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel) {
   return r;
 }
 
-// Byte offset of 16-byte chunk j of row r in a 128B-swizzled K-major tile.
+// Byte offset of 16-byte chunk j of row r in a 128B-swizzled tile (TMA layout).
 __device__ __forceinline__ uint32_t sw128_offset(uint32_t r, uint32_t j) {
   return (r >> 3) * 1024u + (r & 7u) * 128u + ((j ^ (r & 7u)) << 4);
 }
 
 __global__ void __launch_bounds__(kThreads, 1)
     bf_form_beams_tc(const __grid_constant__ CUtensorMap tm_e, const __grid_constant__ CUtensorMap tm_w,
-                     const __grid_constant__ CUtensorMap tm_j, const TcParams p) {
+                     const TcParams p) {
   extern __shared__ uint8_t smem_dyn[];
   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_dyn) + 1023) & ~uintptr_t(1023));
-  const SmemPlan sp = smem_plan(p.stages, p.nb_pass);
-  const int S = p.stages;
-  uint8_t *sA = smem + sp.off_a;
+  const int S = p.stages, SW = p.wslots, R = p.raw;
+  const SmemPlan sp = smem_plan(S, SW, R, p.nb_pass);
   uint8_t *sW = smem + sp.off_w;
   uint8_t *sR = smem + sp.off_r;
-  uint8_t *sJ = smem + sp.off_j;
+  float *sG = reinterpret_cast<float *>(smem + sp.off_g);
   const uint32_t bar0 = smem_u32(smem + sp.off_bar);
-  auto full = [&](int s) { return bar0 + 8u * s; };
-  auto afull = [&](int s) { return bar0 + 8u * (S + s); };
-  auto empty = [&](int s) { return bar0 + 8u * (2 * S + s); };
-  auto accfull = [&](int i) { return bar0 + 8u * (3 * S + i); };
-  auto accempty = [&](int i) { return bar0 + 8u * (3 * S + 2 + i); };
-  uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(smem + sp.off_bar + 8 * (3 * S + 4));
+  auto raw_full = [&](int r) { return bar0 + 8u * r; };
+  auto raw_empty = [&](int r) { return bar0 + 8u * (R + r); };
+  auto w_full = [&](int s) { return bar0 + 8u * (2 * R + s); };
+  auto w_empty = [&](int s) { return bar0 + 8u * (2 * R + SW + s); };
+  auto a_full = [&](int s) { return bar0 + 8u * (2 * R + 2 * SW + s); };
+  auto empty = [&](int s) { return bar0 + 8u * (2 * R + 2 * SW + S + s); };
+  auto accfull = [&](int i) { return bar0 + 8u * (2 * R + 2 * SW + 2 * S + i); };
+  auto accempty = [&](int i) { return bar0 + 8u * (2 * R + 2 * SW + 2 * S + 2 + i); };
+  uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(smem + sp.off_bar + 8 * sp.nbar);
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
+  const int ncols = 2 * p.nb_pass;                     // accumulator columns (GEMM N)
+  const int per_half = (kAccCols - ncols) / kStageCols;  // unpacked stages beside each accumulator
 
   if (threadIdx.x == 0) {
+    for (int r = 0; r < R; ++r) {
+      mbar_init(raw_full(r), 1);
+      mbar_init(raw_empty(r), 128);
+    }
+    for (int s = 0; s < SW; ++s) {
+      mbar_init(w_full(s), 1);
+      mbar_init(w_empty(s), 1);
+    }
     for (int s = 0; s < S; ++s) {
-      mbar_init(full(s), 1);
-      mbar_init(afull(s), 128);
+      mbar_init(a_full(s), 128);
       mbar_init(empty(s), 1);
     }
     for (int i = 0; i < 2; ++i) {
       mbar_init(accfull(i), 1);
-      mbar_init(accempty(i), 128);
+      mbar_init(accempty(i), kEpiThreads);
     }
     fence_barrier_init();
   }
@@ -135,10 +179,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     tmem_alloc(smem_u32(tmem_holder), 2 * kAccCols);
     tmem_relinquish();
   }
-  if (warp == kTmaWarp && lane == 0) {
+  if (warp == kEProdWarp && lane == 0) {
     tma_prefetch_desc(&tm_e);
     tma_prefetch_desc(&tm_w);
-    tma_prefetch_desc(&tm_j);
   }
   tc_fence_before();
   __syncthreads();
@@ -146,41 +189,62 @@ __global__ void __launch_bounds__(kThreads, 1)
   const uint32_t tmem_base = *tmem_holder;
   int *err = p.err;
 
-  if (warp == kTmaWarp) {
-    // ------------------------------------------------------------ producer
+  if (warp == kEProdWarp) {
+    // ------------------------------------------------------------ E producer
     if (lane == 0 && !p.test_stall) {
       const uint64_t pol_e = policy_evict_first();
+      Ring rr(R);
+      uint32_t issued = 0;
+      bool ok = true;
+      for (int tile = blockIdx.x; ok && tile < p.ntiles; tile += gridDim.x) {
+        const int tt = (tile / p.npass) % p.ntt;
+        const int f = tile / (p.npass * p.ntt);
+        for (int ks = 0; ks < p.nk; ++ks, rr.advance(), ++issued) {
+          const int r = static_cast<int>(rr.idx);
+          if (!mbar_wait(raw_empty(r), rr.phase ^ 1u, err, kDevTimeoutEmpty)) {
+            ok = false;
+            break;
+          }
+          mbar_arrive_expect_tx(raw_full(r), kRawBytes);
+          tma_load_3d(smem_u32(sR + r * kRawBytes), &tm_e, raw_full(r), ks * kKC, f, tt * kTT, pol_e);
+        }
+      }
+      if (!ok) {  // let copies already issued land before the CTA exits
+        for (uint32_t k = (issued >= static_cast<uint32_t>(R) ? issued - R : 0); k < issued; ++k)
+          mbar_wait(raw_full(static_cast<int>(k % R)), (k / R) & 1u, err, kDevTimeoutFull);
+      }
+    }
+  } else if (warp == kWProdWarp) {
+    // ------------------------------------------------------------ W producer
+    if (lane == 0 && !p.test_stall) {
       const uint64_t pol_w = policy_evict_last();
-      const uint32_t tx = kRawBytes + sp.wbytes;
+      Ring wr(SW);
       uint32_t it = 0;
       bool ok = true;
       for (int tile = blockIdx.x; ok && tile < p.ntiles; tile += gridDim.x) {
         const int pass = tile % p.npass;
-        const int tt = (tile / p.npass) % p.ntt;
         const int f = tile / (p.npass * p.ntt);
-        for (int ks = 0; ks < p.nk; ++ks, ++it) {
-          const int s = static_cast<int>(it % S);
-          const uint32_t ph = (it / S) & 1u;
-          if (!mbar_wait(empty(s), ph ^ 1u, err, kDevTimeoutEmpty)) {
+        for (int ks = 0; ks < p.nk; ++ks, ++it, wr.advance()) {
+          const int s = static_cast<int>(wr.idx);
+          if (!mbar_wait(w_empty(s), wr.phase ^ 1u, err, kDevTimeoutEmpty)) {
             ok = false;
             break;
           }
-          mbar_arrive_expect_tx(full(s), tx);
-          tma_load_3d(smem_u32(sR + s * kRawBytes), &tm_e, full(s), ks * kKC, f, tt * kTT, pol_e);
-          tma_load_3d(smem_u32(sW + s * sp.wbytes), &tm_w, full(s), ks * kKC, pass * 2 * p.nb_pass, f, pol_w);
+          mbar_arrive_expect_tx(w_full(s), sp.wbytes);
+          tma_load_3d(smem_u32(sW + s * sp.wbytes), &tm_w, w_full(s), ks * kKC, pass * 2 * p.nb_pass, f, pol_w);
         }
       }
-      // On failure, let copies already issued land before the CTA exits.
       if (!ok) {
-        for (uint32_t k = (it >= static_cast<uint32_t>(S) ? it - S : 0); k < it; ++k)
-          mbar_wait(full(static_cast<int>(k % S)), (k / S) & 1u, err, kDevTimeoutFull);
+        for (uint32_t k = (it >= static_cast<uint32_t>(SW) ? it - SW : 0); k < it; ++k)
+          mbar_wait(w_full(static_cast<int>(k % SW)), (k / SW) & 1u, err, kDevTimeoutFull);
       }
     }
   } else if (warp == kMmaWarp) {
     // ------------------------------------------------------------ MMA issuer
     if (lane == 0) {
-      const uint32_t idesc = idesc_e4m3_f32(kBM, 2 * p.nb_pass);
-      uint32_t it = 0, local = 0;
+      const uint32_t idesc = idesc_e4m3_f32(kBM, ncols);
+      Ring ar(S), wr(SW);
+      uint32_t local = 0;
       bool ok = true;
       for (int tile = blockIdx.x; ok && tile < p.ntiles; tile += gridDim.x, ++local) {
         const uint32_t ab = local & 1u;
@@ -188,22 +252,24 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (!mbar_wait(accempty(ab), aph ^ 1u, err, kDevTimeoutAccEmpty)) break;
         tc_fence_after();
         const uint32_t d_tmem = tmem_base + ab * kAccCols;
-        for (int ks = 0; ks < p.nk; ++ks, ++it) {
-          const int s = static_cast<int>(it % S);
-          const uint32_t ph = (it / S) & 1u;
-          if (!mbar_wait(afull(s), ph, err, kDevTimeoutUnpacked) || !mbar_wait(full(s), ph, err, kDevTimeoutFull)) {
+        for (int ks = 0; ks < p.nk; ++ks, ar.advance(), wr.advance()) {
+          const int s = static_cast<int>(ar.idx);
+          const int sw = static_cast<int>(wr.idx);
+          if (!mbar_wait(a_full(s), ar.phase, err, kDevTimeoutUnpacked) ||
+              !mbar_wait(w_full(sw), wr.phase, err, kDevTimeoutFull)) {
             ok = false;
             break;
           }
           tc_fence_after();
-          const uint32_t a_base = smem_u32(sA + s * kABytes);
-          const uint32_t b_base = smem_u32(sW + s * sp.wbytes);
+          const uint32_t a_tmem = tmem_base + stage_col(s, ncols, per_half);
+          const uint32_t b_base = smem_u32(sW + sw * sp.wbytes);
 #pragma unroll
           for (int kk = 0; kk < kKC / 32; ++kk) {
-            mma_f8f6f4(d_tmem, smem_desc_sw128(a_base + 32 * kk), smem_desc_sw128(b_base + 32 * kk), idesc,
-                       (ks | kk) != 0 ? 1u : 0u);
+            mma_f8f6f4_ts(d_tmem, a_tmem + 8 * kk, smem_desc_sw128(b_base + 32 * kk), idesc,
+                          (ks | kk) != 0 ? 1u : 0u);
           }
           mma_commit(empty(s));
+          mma_commit(w_empty(sw));
         }
         if (!ok) break;
         mma_commit(accfull(ab));
@@ -211,46 +277,91 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
   } else if (warp >= kUnpackWarp0) {
     // ------------------------------------------------------------ unpack
-    const int uw = warp - kUnpackWarp0;
-    const uint32_t tl = 32u * (uw & 1) + lane;   // time within the tile
-    const uint32_t jbase = 4u * (uw >> 1);       // 16-byte chunks jbase..jbase+3
-    const uint32_t row0 = tl, row1 = 64u + tl;  // GEMM rows (p=0, t) and (p=1, t)
-    uint32_t it = 0;
+    // Group g (warps 11-14 or 15-18) takes the K stages with it % 2 == g.  Lane
+    // pair (2u, 2u+1) of quarter q holds rows (t, p=0) and (t, p=1) of time
+    // t = 16q + u: both lanes read the raw row and keep their polarization.
+    const int group = (warp - kUnpackWarp0) >> 2;
+    const int q = warp & 3;
+    const uint32_t pp = lane & 1u;
+    const uint32_t tl = 16u * q + (lane >> 1);
+    const uint32_t lane_addr = static_cast<uint32_t>(32 * q) << 16;
+    const uint32_t sel = pp ? 0x7531u : 0x6420u;  // odd or even bytes: polarization 1 or 0
+    // this CTA's K stages: tiles blockIdx.x, blockIdx.x + gridDim.x, ... times nk; group g takes every other
+    const uint32_t my_tiles =
+        static_cast<int>(blockIdx.x) < p.ntiles ? (p.ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0u;
+    const uint32_t total = my_tiles * static_cast<uint32_t>(p.nk);
+    Ring rr(R), ar(S);
+    if (group) {
+      rr.advance();
+      ar.advance();
+    }
     bool ok = true;
-    for (int tile = blockIdx.x; ok && tile < p.ntiles; tile += gridDim.x) {
-      for (int ks = 0; ks < p.nk; ++ks, ++it) {
-        const int s = static_cast<int>(it % S);
-        const uint32_t ph = (it / S) & 1u;
-        if (!mbar_wait(full(s), ph, err, kDevTimeoutFull)) {
+    for (uint32_t it = group; ok && it < total; it += 2, rr.advance(), rr.advance(), ar.advance(), ar.advance()) {
+      {
+        const int r = static_cast<int>(rr.idx);
+        const int s = static_cast<int>(ar.idx);
+        if (!__all_sync(0xffffffffu, mbar_wait(raw_full(r), rr.phase, err, kDevTimeoutFull))) {
+          ok = false;  // the warp leaves together
+          break;
+        }
+        const uint8_t *raw = sR + r * kRawBytes;
+        uint32_t e[16];  // this lane's polarization, dishes 4m..4m+3 in word m
+#pragma unroll
+        for (uint32_t j = 0; j < 8; ++j) {
+          // 16-byte chunk j: dishes 8j..8j+7, bytes [d0p0 d0p1 d1p0 d1p1 ...]
+          const uint4 w = *reinterpret_cast<const uint4 *>(raw + sw128_offset(tl, j));
+          e[2 * j] = prmt(w.x, w.y, sel);
+          e[2 * j + 1] = prmt(w.z, w.w, sel);
+        }
+        mbar_arrive(raw_empty(r));  // the raw slot is in registers now
+        uint32_t out[32];
+        const uint32_t msk = 0x0F0F0F0Fu;
+#pragma unroll
+        for (int m = 0; m < 16; ++m) {
+          out[2 * m] = (e[m] >> 4) & msk;  // real nibbles u (E4M3 bytes = u * 2^-9)
+          out[2 * m + 1] = e[m] & msk;     // imaginary nibbles
+        }
+        // only now wait for the tensor core to release this operand stage
+        if (!__all_sync(0xffffffffu, mbar_wait(empty(s), ar.phase ^ 1u, err, kDevTimeoutEmpty))) {
           ok = false;
           break;
         }
-        const uint8_t *raw = sR + s * kRawBytes;
-        uint8_t *a = sA + s * kABytes;
-#pragma unroll
-        for (uint32_t jj = 0; jj < 4; ++jj) {
-          const uint32_t j = jbase + jj;
-          // 8 dishes x 2 polarizations: bytes [d0p0 d0p1 d1p0 d1p1 ... d7p1]
-          const uint4 w = *reinterpret_cast<const uint4 *>(raw + sw128_offset(tl, j));
-          const uint32_t x0 = prmt(w.x, w.y, 0x6420u), y0 = prmt(w.x, w.y, 0x7531u);  // d0-3, p0 / p1
-          const uint32_t x1 = prmt(w.z, w.w, 0x6420u), y1 = prmt(w.z, w.w, 0x7531u);  // d4-7, p0 / p1
-          const uint32_t m = 0x0F0F0F0Fu;
-          // k order inside the chunk: re(d0-3) im(d0-3) re(d4-7) im(d4-7)
-          const uint4 o0 = make_uint4((x0 >> 4) & m, x0 & m, (x1 >> 4) & m, x1 & m);
-          const uint4 o1 = make_uint4((y0 >> 4) & m, y0 & m, (y1 >> 4) & m, y1 & m);
-          *reinterpret_cast<uint4 *>(a + sw128_offset(row0, j)) = o0;
-          *reinterpret_cast<uint4 *>(a + sw128_offset(row1, j)) = o1;
-        }
-        fence_proxy_async_smem();
-        mbar_arrive(afull(s));
+        tmem_st_32x32b_x32(tmem_base + lane_addr + stage_col(s, ncols, per_half), out);
+        tmem_st_wait();
+        tc_fence_before();
+        mbar_arrive(a_full(s));
       }
     }
   } else {
     // ------------------------------------------------------------ epilogue
-    const int q = warp;                       // TMEM lane quarter
-    const uint32_t pol = static_cast<uint32_t>(q) >> 1;
-    const uint32_t tl = 32u * (q & 1) + lane;
+    // Warp w reads TMEM lane quarter w % 4 (times 16q..16q+15, both
+    // polarizations interleaved by lane) and column half w / 4.
+    const int q = warp & 3;
+    const int half = warp >> 2;
+    const uint32_t pol = lane & 1u;
     const uint32_t lane_addr = static_cast<uint32_t>(32 * q) << 16;
+    const uint32_t j4 = (lane >> 1) & 3u;  // position among the 4 lanes of equal polarization
+    const uint32_t g4 = lane >> 3;         // group of 4 consecutive times
+    // byte-transpose selectors: 4 lanes x 4 beams -> each lane holds one beam's 4 times
+    const uint32_t sel1 = (j4 & 1) ? 0x3715u : 0x6240u;
+    const uint32_t sel2 = (j4 & 2) ? 0x3276u : 0x5410u;
+    const int nchunk = p.nb_pass / 8;
+    const int c_mid = (nchunk + 1) / 2;
+    const int c_begin = half ? c_mid : 0, c_end = half ? nchunk : c_mid;
+    const int ng = 3 * p.nb_pass;  // floats per gain buffer
+    const float kMagic = 12582920.0f;  // 1.5 * 2^23 + 8: x + kMagic has rint(x) + 8 in its low mantissa bits
+
+    // gains and row sums of one (frequency, beam pass): value i of the buffer
+    auto gain_value = [&](int tile, int i) -> float {
+      const int pass = tile % p.npass;
+      const int f = tile / (p.npass * p.ntt);
+      const int b0 = pass * p.nb_pass;
+      if (i < p.nb_pass) return (b0 + i < p.B) ? __ldg(p.G + static_cast<int64_t>(f) * p.B + b0 + i) : 0.0f;
+      return __ldg(p.bias + static_cast<int64_t>(f) * p.nw_pad + 2 * b0 + (i - p.nb_pass));
+    };
+    if (static_cast<int>(blockIdx.x) < p.ntiles)
+      for (int i = threadIdx.x; i < ng; i += kEpiThreads) sG[i] = gain_value(blockIdx.x, i);
+
     uint32_t local = 0;
     for (int tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x, ++local) {
       const int pass = tile % p.npass;
@@ -258,42 +369,100 @@ __global__ void __launch_bounds__(kThreads, 1)
       const int f = tile / (p.npass * p.ntt);
       const uint32_t ab = local & 1u;
       const uint32_t aph = (local >> 1) & 1u;
-      uint8_t *js = sJ + ab * sp.jbytes;
-      if (threadIdx.x == 0) bulk_wait_group_read<1>();  // the store that used this buffer has read it
-      named_bar_sync(1, 128);
-      const bool got = mbar_wait(accfull(ab), aph, err, kDevTimeoutAccFull);
-      if (!named_bar_and(2, 128, got)) break;  // all four warps leave together
-      tc_fence_after();
       const int b0 = pass * p.nb_pass;
-      const float *g = p.G + static_cast<int64_t>(f) * p.B;
-      const float *bias = p.bias + static_cast<int64_t>(f) * p.nw_pad + 2 * b0;
-      for (int c = 0; c < p.nb_pass / 8; ++c) {
-        uint32_t r[16];
-        tmem_ld_32x32b_x16(tmem_base + ab * kAccCols + lane_addr + 16u * c, r);
-        tmem_ld_wait();
+      const float *gcur = sG + (local & 1u) * ng;
+      float *gnext = sG + ((local + 1) & 1u) * ng;
+      named_bar_sync(1, kEpiThreads);  // this tile's gains are written; last tile's readers are done
+      // next tile's gains: loads in flight during this tile, stored at its end
+      const int next = tile + static_cast<int>(gridDim.x);
+      float pre[2] = {0.0f, 0.0f};
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const int i = static_cast<int>(threadIdx.x) + k * kEpiThreads;
+        if (next < p.ntiles && i < ng) pre[k] = gain_value(next, i);
+      }
+      const bool got = mbar_wait(accfull(ab), aph, err, kDevTimeoutAccFull);
+      if (!named_bar_and(2, kEpiThreads, got)) break;  // all eight warps leave together
+      tc_fence_after();
+      const int64_t t = static_cast<int64_t>(tt) * kTT + 16 * q + 4 * g4;  // first of this lane's 4 times
+      const bool t_ok = t < p.T;
+      const uint32_t acc_addr = tmem_base + ab * kAccCols + lane_addr;
+
+      auto process = [&](int c, const uint32_t (&r)[16]) {
+        const float4 ga = *reinterpret_cast<const float4 *>(gcur + 8 * c);
+        const float4 gb = *reinterpret_cast<const float4 *>(gcur + 8 * c + 4);
+        const float *bs = gcur + p.nb_pass + 16 * c;
+        const float4 bra = *reinterpret_cast<const float4 *>(bs);
+        const float4 brb = *reinterpret_cast<const float4 *>(bs + 4);
+        const float4 bia = *reinterpret_cast<const float4 *>(bs + 8);
+        const float4 bib = *reinterpret_cast<const float4 *>(bs + 12);
+        const float gv[8] = {ga.x, ga.y, ga.z, ga.w, gb.x, gb.y, gb.z, gb.w};
+        const float br[8] = {bra.x, bra.y, bra.z, bra.w, brb.x, brb.y, brb.z, brb.w};
+        const float bi[8] = {bia.x, bia.y, bia.z, bia.w, bib.x, bib.y, bib.z, bib.w};
+        uint32_t qre[8], qim[8];
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
-          const int bl = 8 * c + i;
-          const int b = b0 + bl;
-          const float gb = b < p.B ? __ldg(g + b) : 0.0f;
-          // exact integer sums: 512 * acc - 8 * sum(W), both below 2^24
-          const float raw_re = fmaf(__uint_as_float(r[i]), 512.0f, -__ldg(bias + 16 * c + i));
-          const float raw_im = fmaf(__uint_as_float(r[8 + i]), 512.0f, -__ldg(bias + 16 * c + 8 + i));
-          const int jre = max(-7, min(7, __float2int_rn(__fmul_rn(gb, raw_re))));
-          const int jim = max(-7, min(7, __float2int_rn(__fmul_rn(gb, raw_im))));
-          js[(bl * 2 + pol) * kTT + tl] = static_cast<uint8_t>(((jre + 8) << 4) | (jim + 8));
+          // raw = 512 * acc - 8 * sum(W): exact integers below 2^24
+          const float raw_re = fmaf(__uint_as_float(r[i]), 512.0f, -br[i]);
+          const float raw_im = fmaf(__uint_as_float(r[8 + i]), 512.0f, -bi[i]);
+          // clamp(lrint(G * float(raw)), -7, 7) + 8: one IEEE multiply, clamp to +-7.25
+          // (same result after rounding), round half to even by adding kMagic
+          const float yre = fminf(fmaxf(__fmul_rn(gv[i], raw_re), -7.25f), 7.25f);
+          const float yim = fminf(fmaxf(__fmul_rn(gv[i], raw_im), -7.25f), 7.25f);
+          qre[i] = __float_as_uint(__fadd_rn(yre, kMagic));  // low byte = Jre + 8
+          qim[i] = __float_as_uint(__fadd_rn(yim, kMagic));  // low byte = Jim + 8
+        }
+        // ucomplex4 bytes of beams 0-3 and 4-7 for this lane's time
+        uint32_t w[2];
+#pragma unroll
+        for (int h2 = 0; h2 < 2; ++h2) {
+          const uint32_t rr = prmt(prmt(qre[4 * h2], qre[4 * h2 + 1], 0x0040u),
+                                   prmt(qre[4 * h2 + 2], qre[4 * h2 + 3], 0x0040u), 0x5410u);
+          const uint32_t ii = prmt(prmt(qim[4 * h2], qim[4 * h2 + 1], 0x0040u),
+                                   prmt(qim[4 * h2 + 2], qim[4 * h2 + 3], 0x0040u), 0x5410u);
+          const uint32_t x = rr * 16u + ii;  // (re nibble << 4) | im nibble, per byte
+          const uint32_t x1 = prmt(x, __shfl_xor_sync(0xffffffffu, x, 2), sel1);
+          w[h2] = prmt(x1, __shfl_xor_sync(0xffffffffu, x1, 4), sel2);  // beam 4*h2 + j4, times t..t+3
+        }
+        if (t_ok) {
+#pragma unroll
+          for (int h2 = 0; h2 < 2; ++h2) {
+            const int b = b0 + 8 * c + 4 * h2 + static_cast<int>(j4);
+            if (b < p.B) {
+              // J[b][f][p][t..t+3] (Jlinear, arraysizes.hxx:92)
+              uint32_t *dst = reinterpret_cast<uint32_t *>(
+                  p.J + ((static_cast<int64_t>(b) * p.F + f) * 2 + pol) * p.T + t);
+              __stcs(dst, w[h2]);
+            }
+          }
+        }
+      };
+
+      // accumulator columns in chunks of 16, the next chunk's TMEM load in flight
+      uint32_t ra[16], rb[16];
+      if (c_begin < c_end) {
+        tmem_ld_32x32b_x16(acc_addr + 16u * c_begin, ra);
+        tmem_ld_wait(ra);
+      }
+      for (int c = c_begin; c < c_end; c += 2) {
+        const bool has1 = c + 1 < c_end, has2 = c + 2 < c_end;
+        if (has1) tmem_ld_32x32b_x16(acc_addr + 16u * (c + 1), rb);
+        process(c, ra);
+        if (has1) {
+          tmem_ld_wait(rb);
+          if (has2) tmem_ld_32x32b_x16(acc_addr + 16u * (c + 2), ra);
+          process(c + 1, rb);
+          if (has2) tmem_ld_wait(ra);
         }
       }
       tc_fence_before();
       mbar_arrive(accempty(ab));
-      fence_proxy_async_smem();
-      named_bar_sync(1, 128);
-      if (threadIdx.x == 0) {
-        tma_store_4d(&tm_j, smem_u32(js), tt * kTT, 0, f, b0);
-        bulk_commit_group();
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const int i = static_cast<int>(threadIdx.x) + k * kEpiThreads;
+        if (next < p.ntiles && i < ng) gnext[i] = pre[k];
       }
     }
-    if (threadIdx.x == 0) bulk_wait_group<0>();
   }
 
   tc_fence_before();
@@ -372,6 +541,8 @@ bool make_map(CUtensorMap *m, const void *base, int rank, const cuuint64_t *dims
 }
 
 int g_test_stall = 0;
+int g_plan_wslots = 0;  // nonzero: W slots to use (tuning)
+int g_plan_raw = 0;     // nonzero: raw E slots to use (tuning)
 
 int num_sms() {
   static int n = 0;
@@ -388,9 +559,18 @@ int num_sms() {
 
 void tc_set_test_stall(int on) { g_test_stall = on; }
 
+void tc_set_ring_plan(int wslots, int raw) {
+  g_plan_wslots = wslots;
+  g_plan_raw = raw;
+}
+
 void tc_plan_beams(int64_t B, int *nb_pass, int *npass) {
+  // at most 96 beams (192 accumulator columns) per pass, so that two
+  // accumulators and at least four unpacked stages fit the 512 TMEM columns;
+  // passes are balanced
   const int64_t b8 = (B + 7) / 8 * 8;
-  const int64_t nbp = std::min<int64_t>(b8, 128);
+  const int64_t np = (b8 + 95) / 96;
+  const int64_t nbp = ((b8 + np - 1) / np + 7) / 8 * 8;
   *nb_pass = static_cast<int>(nbp);
   *npass = static_cast<int>((b8 + nbp - 1) / nbp);
 }
@@ -420,6 +600,7 @@ cudaError_t launch_tc(const TcWeights &w, int64_t T, uint8_t *J, const uint8_t *
   p.F = static_cast<int>(F);
   p.D = static_cast<int>(D);
   p.B = static_cast<int>(B);
+  p.J = J;
   p.nb_pass = w.nb_pass;
   p.npass = w.npass;
   p.ntt = static_cast<int>((T + kTT - 1) / kTT);
@@ -432,13 +613,26 @@ cudaError_t launch_tc(const TcWeights &w, int64_t T, uint8_t *J, const uint8_t *
   p.bias = w.bias;
   p.err = err;
   p.test_stall = g_test_stall;
-  int stages = kMaxStages;
-  while (stages > 2 && smem_plan(stages, w.nb_pass).total + 1024 > kSmemLimit) --stages;
+  // unpacked stages live in the TMEM columns beside the two accumulators; raw E
+  // slots take the shared memory the W slots leave
+  const int per_half = (kAccCols - 2 * w.nb_pass) / kStageCols;
+  const int stages = std::min(kMaxStages, 2 * per_half);
+  if (stages < 2) return cudaErrorInvalidValue;
+  // shared memory: W slots first (their loads gate the MMA), then raw E slots
+  int wslots = g_plan_wslots > 0 ? g_plan_wslots : kMaxWSlots;
+  int raw = g_plan_raw > 0 ? g_plan_raw : kMinRaw;
+  while (wslots > 2 && smem_plan(stages, wslots, raw, w.nb_pass).total + 1024 > kSmemLimit) --wslots;
+  while (raw < kMaxRaw && smem_plan(stages, wslots, raw + 1, w.nb_pass).total + 1024 <= kSmemLimit &&
+         g_plan_raw <= 0)
+    ++raw;
+  while (raw > 2 && smem_plan(stages, wslots, raw, w.nb_pass).total + 1024 > kSmemLimit) --raw;
   p.stages = stages;
-  const int smem_bytes = smem_plan(stages, w.nb_pass).total + 1024;
+  p.wslots = wslots;
+  p.raw = raw;
+  const int smem_bytes = smem_plan(stages, wslots, raw, w.nb_pass).total + 1024;
   if (smem_bytes > kSmemLimit) return cudaErrorInvalidValue;
 
-  CUtensorMap tm_e, tm_w, tm_j;
+  CUtensorMap tm_e, tm_w;
   {  // E[t][f][d*p] bytes: dims {2D, F, T}
     const cuuint64_t dims[3] = {static_cast<cuuint64_t>(2 * D), static_cast<cuuint64_t>(F),
                                 static_cast<cuuint64_t>(T)};
@@ -453,15 +647,6 @@ cudaError_t launch_tc(const TcWeights &w, int64_t T, uint8_t *J, const uint8_t *
     const cuuint32_t box[3] = {static_cast<cuuint32_t>(kKC), static_cast<cuuint32_t>(2 * w.nb_pass), 1};
     if (!make_map(&tm_w, w.W, 3, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B)) return cudaErrorInvalidValue;
   }
-  {  // J[b][f][p][t] bytes: dims {T, 2, F, B}
-    const cuuint64_t dims[4] = {static_cast<cuuint64_t>(T), 2, static_cast<cuuint64_t>(F),
-                                static_cast<cuuint64_t>(B)};
-    const cuuint64_t str[3] = {static_cast<cuuint64_t>(T), static_cast<cuuint64_t>(2 * T),
-                               static_cast<cuuint64_t>(2 * T * F)};
-    const cuuint32_t box[4] = {static_cast<cuuint32_t>(kTT), 2, 1, static_cast<cuuint32_t>(w.nb_pass)};
-    if (!make_map(&tm_j, J, 4, dims, str, box, CU_TENSOR_MAP_SWIZZLE_NONE)) return cudaErrorInvalidValue;
-  }
-
   static bool attr_set = false;
   if (!attr_set) {
     const cudaError_t e =
@@ -471,7 +656,7 @@ cudaError_t launch_tc(const TcWeights &w, int64_t T, uint8_t *J, const uint8_t *
   }
   const int grid = static_cast<int>(std::min<int64_t>(ntiles, num_sms()));
   if (grid <= 0) return cudaSuccess;
-  bf_form_beams_tc<<<grid, kThreads, smem_bytes, s>>>(tm_e, tm_w, tm_j, p);
+  bf_form_beams_tc<<<grid, kThreads, smem_bytes, s>>>(tm_e, tm_w, p);
   return cudaGetLastError();
 }
 

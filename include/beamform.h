@@ -152,7 +152,7 @@ BF_API int bf_form_beams_resident(const bf_weights *w, int64_t ntimes, uint8_t *
  * (npolarizations == 2, ndishes % 8 == 0, ntimes % 16 == 0, E and J 16-byte
  * aligned; else BF_ERR_UNSUPPORTED) and
  *   256 + roundup256(4 * F * npass * 2 * nb) + F * 2 * roundup(B, 8) * 2 * D <= 4 MiB
- * (nb = min(roundup(B, 8), 128), npass = ceil(roundup(B, 8) / nb); else
+ * (npass = ceil(roundup(B, 8) / 96), nb = roundup(ceil(roundup(B, 8) / npass), 8); else
  * BF_ERR_TOO_LARGE) -- e.g. f=16, b=96, d=512 fits, f=84 does not.
  * Synchronous: returns once the pass on `stream` has finished, with its status.
  * The first call on a device looks up the array's device address; make that
