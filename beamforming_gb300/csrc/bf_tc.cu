@@ -54,14 +54,17 @@ constexpr int kWProdWarp = 10;
 constexpr int kUnpackWarp0 = 11;        // warps 11-18: two groups, each covering TMEM lane quarters 3, 0, 1, 2
 constexpr int kTT = 64;                 // times per tile
 constexpr int kBM = 128;                // GEMM rows per tile
-constexpr int kKC = 128;                // K bytes per stage (64 dishes x re/im)
-constexpr int kRawBytes = kTT * kKC;    // raw E per stage: 64 times x 64 dishes x 2 pol
+constexpr int kKC = 128;                // K bytes per TMA box / swizzle atom (64 dishes x re/im)
+constexpr int kSub = 2;                 // boxes per pipeline stage
+constexpr int kStageK = kSub * kKC;     // K bytes per stage (128 dishes x re/im): 8 MMAs
+constexpr int kRawBox = kTT * kKC;      // raw E per box: 64 times x 64 dishes x 2 pol
+constexpr int kRawBytes = kSub * kRawBox;
 constexpr int kAccCols = 256;           // TMEM column offset of the second accumulator
-constexpr int kStageCols = kKC / 4;     // TMEM columns per unpacked stage
+constexpr int kStageCols = kStageK / 4;  // TMEM columns per unpacked stage
 constexpr int kSmemLimit = 232448;      // 227 KiB opt-in per block
 constexpr int kMaxStages = 8;
 constexpr int kMaxWSlots = 6;
-constexpr int kMinRaw = 8;
+constexpr int kMinRaw = 4;
 constexpr int kMaxRaw = 16;
 
 struct TcParams {
@@ -83,13 +86,14 @@ struct TcParams {
 };
 
 struct SmemPlan {
-  int wbytes;
+  int wbox, wbytes;
   int off_w, off_r, off_g, off_bar, nbar, total;
 };
 
 __host__ __device__ inline SmemPlan smem_plan(int stages, int wslots, int raw, int nb_pass) {
   SmemPlan s{};
-  s.wbytes = 2 * nb_pass * kKC;
+  s.wbox = 2 * nb_pass * kKC;
+  s.wbytes = kSub * s.wbox;
   s.off_w = 0;
   s.off_r = s.off_w + wslots * s.wbytes;
   // two buffers of gains [nb_pass] + row sums [2 * nb_pass]: this tile's and the next tile's
@@ -206,7 +210,10 @@ __global__ void __launch_bounds__(kThreads, 1)
             break;
           }
           mbar_arrive_expect_tx(raw_full(r), kRawBytes);
-          tma_load_3d(smem_u32(sR + r * kRawBytes), &tm_e, raw_full(r), ks * kKC, f, tt * kTT, pol_e);
+#pragma unroll
+          for (int h = 0; h < kSub; ++h)
+            tma_load_3d(smem_u32(sR + r * kRawBytes + h * kRawBox), &tm_e, raw_full(r), (ks * kSub + h) * kKC, f,
+                        tt * kTT, pol_e);
         }
       }
       if (!ok) {  // let copies already issued land before the CTA exits
@@ -231,7 +238,10 @@ __global__ void __launch_bounds__(kThreads, 1)
             break;
           }
           mbar_arrive_expect_tx(w_full(s), sp.wbytes);
-          tma_load_3d(smem_u32(sW + s * sp.wbytes), &tm_w, w_full(s), ks * kKC, pass * 2 * p.nb_pass, f, pol_w);
+#pragma unroll
+          for (int h = 0; h < kSub; ++h)
+            tma_load_3d(smem_u32(sW + s * sp.wbytes + h * sp.wbox), &tm_w, w_full(s), (ks * kSub + h) * kKC,
+                        pass * 2 * p.nb_pass, f, pol_w);
         }
       }
       if (!ok) {
@@ -262,11 +272,12 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
           tc_fence_after();
           const uint32_t a_tmem = tmem_base + stage_col(s, ncols, per_half);
-          const uint32_t b_base = smem_u32(sW + sw * sp.wbytes);
+          const uint64_t b_desc = smem_desc_sw128(smem_u32(sW + sw * sp.wbytes));
 #pragma unroll
-          for (int kk = 0; kk < kKC / 32; ++kk) {
-            mma_f8f6f4_ts(d_tmem, a_tmem + 8 * kk, smem_desc_sw128(b_base + 32 * kk), idesc,
-                          (ks | kk) != 0 ? 1u : 0u);
+          for (int kk = 0; kk < kStageK / 32; ++kk) {
+            // K step kk: box kk / 4, 32 bytes into its 128-byte rows (descriptor address field is in 16 B units)
+            const uint64_t off = static_cast<uint64_t>(((kk >> 2) * sp.wbox + 32 * (kk & 3)) >> 4);
+            mma_f8f6f4_ts(d_tmem, a_tmem + 8 * kk, b_desc + off, idesc, (ks | kk) != 0 ? 1u : 0u);
           }
           mma_commit(empty(s));
           mma_commit(w_empty(sw));
@@ -304,29 +315,38 @@ __global__ void __launch_bounds__(kThreads, 1)
           ok = false;  // the warp leaves together
           break;
         }
-        const uint8_t *raw = sR + r * kRawBytes;
-        uint32_t e[16];  // this lane's polarization, dishes 4m..4m+3 in word m
+        const uint32_t col = tmem_base + lane_addr + stage_col(s, ncols, per_half);
+        bool slot_ok = true;
 #pragma unroll
-        for (uint32_t j = 0; j < 8; ++j) {
-          // 16-byte chunk j: dishes 8j..8j+7, bytes [d0p0 d0p1 d1p0 d1p1 ...]
-          const uint4 w = *reinterpret_cast<const uint4 *>(raw + sw128_offset(tl, j));
-          e[2 * j] = prmt(w.x, w.y, sel);
-          e[2 * j + 1] = prmt(w.z, w.w, sel);
-        }
-        mbar_arrive(raw_empty(r));  // the raw slot is in registers now
-        uint32_t out[32];
-        const uint32_t msk = 0x0F0F0F0Fu;
+        for (int h = 0; h < kSub; ++h) {
+          const uint8_t *raw = sR + r * kRawBytes + h * kRawBox;
+          uint32_t e[16];  // this lane's polarization, dishes 4m..4m+3 of the box in word m
 #pragma unroll
-        for (int m = 0; m < 16; ++m) {
-          out[2 * m] = (e[m] >> 4) & msk;  // real nibbles u (E4M3 bytes = u * 2^-9)
-          out[2 * m + 1] = e[m] & msk;     // imaginary nibbles
+          for (uint32_t j = 0; j < 8; ++j) {
+            // 16-byte chunk j: dishes 8j..8j+7, bytes [d0p0 d0p1 d1p0 d1p1 ...]
+            const uint4 w = *reinterpret_cast<const uint4 *>(raw + sw128_offset(tl, j));
+            e[2 * j] = prmt(w.x, w.y, sel);
+            e[2 * j + 1] = prmt(w.z, w.w, sel);
+          }
+          if (h == kSub - 1) mbar_arrive(raw_empty(r));  // the raw slot is in registers now
+          uint32_t out[32];
+          const uint32_t msk = 0x0F0F0F0Fu;
+#pragma unroll
+          for (int m = 0; m < 16; ++m) {
+            out[2 * m] = (e[m] >> 4) & msk;  // real nibbles u (E4M3 bytes = u * 2^-9)
+            out[2 * m + 1] = e[m] & msk;     // imaginary nibbles
+          }
+          if (h == 0) {
+            // only now wait for the tensor core to release this operand stage
+            slot_ok = __all_sync(0xffffffffu, mbar_wait(empty(s), ar.phase ^ 1u, err, kDevTimeoutEmpty));
+            if (!slot_ok) break;
+          }
+          tmem_st_32x32b_x32(col + 32 * h, out);
         }
-        // only now wait for the tensor core to release this operand stage
-        if (!__all_sync(0xffffffffu, mbar_wait(empty(s), ar.phase ^ 1u, err, kDevTimeoutEmpty))) {
+        if (!slot_ok) {
           ok = false;
           break;
         }
-        tmem_st_32x32b_x32(tmem_base + lane_addr + stage_col(s, ncols, per_half), out);
         tmem_st_wait();
         tc_fence_before();
         mbar_arrive(a_full(s));
@@ -604,7 +624,7 @@ cudaError_t launch_tc(const TcWeights &w, int64_t T, uint8_t *J, const uint8_t *
   p.nb_pass = w.nb_pass;
   p.npass = w.npass;
   p.ntt = static_cast<int>((T + kTT - 1) / kTT);
-  p.nk = static_cast<int>((D + 63) / 64);
+  p.nk = static_cast<int>((D + kStageK / 2 - 1) / (kStageK / 2));
   const int64_t ntiles = static_cast<int64_t>(p.ntt) * F * p.npass;
   if (ntiles > 0x7FFFFFFF) return cudaErrorInvalidValue;
   p.ntiles = static_cast<int>(ntiles);
