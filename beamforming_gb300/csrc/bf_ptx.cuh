@@ -63,23 +63,32 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
   return ok != 0;
 }
 
+// try_wait that lets the hardware suspend the thread until the phase completes
+// or `hint_ns` nanoseconds pass, so waiting warps do not take issue slots.
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint32_t bar, uint32_t parity, uint32_t hint_ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity), "r"(hint_ns)
+      : "memory");
+  return ok != 0;
+}
+
 // Bounded wait for the phase with the given parity to complete.  Returns false
 // (after recording `code` in *err) when no progress was seen for
 // kWaitTimeoutNs, or when another role of the kernel already failed.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int *err, int code) {
   if (mbar_try_wait(bar, parity)) return true;
-  uint64_t t0 = 0;
-  for (uint32_t i = 1;; ++i) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if ((i & 255u) == 0) {
-      if (*reinterpret_cast<volatile int *>(err) != 0) return false;
-      const uint64_t now = globaltimer_ns();
-      if (t0 == 0) {
-        t0 = now;
-      } else if (now - t0 > kWaitTimeoutNs) {
-        atomicCAS(err, 0, code);
-        return false;
-      }
+  const uint64_t t0 = globaltimer_ns();
+  for (;;) {
+    if (mbar_try_wait_sleep(bar, parity, 200000u)) return true;
+    if (*reinterpret_cast<volatile int *>(err) != 0) return false;
+    if (globaltimer_ns() - t0 > kWaitTimeoutNs) {
+      atomicCAS(err, 0, code);
+      return false;
     }
   }
 }

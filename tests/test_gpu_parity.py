@@ -180,6 +180,20 @@ def test_half_way_rounding(bflib, cuda, oracle):
         np.testing.assert_array_equal(J, oracle.form_beams(oracle_dims(oracle, d), E, A, G), err_msg=kernel)
 
 
+@pytest.mark.parametrize("scale", [1e-4, 0.3, 7.0, 1e4])
+def test_gain_ranges(bflib, cuda, oracle, scale):
+    """Gains from tiny to huge, both signs: covers the packed 16-bit clamp
+    (small |G| * |raw|) and the single-precision clamp (large) of the epilogue."""
+    d = bflib.Dims(192, 3, 512, 2, 40)
+    E, A, _ = bflib.seeded_host_inputs(d, 21)
+    rng = np.random.default_rng(int(scale * 10) + 1)
+    G = (rng.uniform(-1, 1, d.gsize) * scale).astype(np.float32)
+    G[::7] = np.float32(0.0)
+    for kernel in ("tensor", "simt"):
+        J = run_gpu(bflib, cuda, d, E, A, G, kernel)
+        np.testing.assert_array_equal(J, oracle.form_beams(oracle_dims(oracle, d), E, A, G), err_msg=kernel)
+
+
 def test_impulse(bflib, cuda, oracle):
     """cuda4.cu:1325-1412 impulse construction with a fixed seed: one nonzero
     A, E and G; J = G*A*E at one (b,f,p,t) and zero elsewhere."""
