@@ -9,6 +9,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <thread>
@@ -49,9 +50,20 @@ struct DevBuf {
   }
 };
 
+// One pipeline lane of the host-pointer path: a stream and the E chunk in flight on it.
+struct Lane {
+  cudaStream_t s = nullptr;
+  cudaEvent_t done = nullptr;
+  DevBuf E;
+};
+
+constexpr int kLanes = 3;
+
 struct DeviceCtx {
   std::mutex mu;
   bool ready = false;
+  bool lanes_ready = false;
+  Lane lanes[kLanes];
   int *err = nullptr;       // device error word written by kernels
   uint32_t *adler = nullptr;  // device adler32 result
   DevBuf E, A, G, J;        // staging for host-pointer calls
@@ -125,9 +137,18 @@ int choose_tensor(const bf_dims &d, bool *use_tc) {
   return BF_OK;
 }
 
+// All four arrays on the device; the tensor-core operand goes to W / bias.
+int run_device_bufs(const bf_dims &d, uint8_t *J, const uint8_t *E, const uint8_t *A, const float *G, DevBuf &W,
+                    DevBuf &bias, int *err, cudaStream_t s);
+
 // All four arrays on the device.  Operand scratch comes from ctx (caller holds ctx.mu).
 int run_device(DeviceCtx &c, const bf_dims &d, uint8_t *J, const uint8_t *E, const uint8_t *A, const float *G,
                cudaStream_t s) {
+  return run_device_bufs(d, J, E, A, G, c.W, c.bias, c.err, s);
+}
+
+int run_device_bufs(const bf_dims &d, uint8_t *J, const uint8_t *E, const uint8_t *A, const float *G, DevBuf &Wb,
+                    DevBuf &biasb, int *err, cudaStream_t s) {
   if (jsize(d) == 0) return BF_OK;
   bool use_tc = false;
   const int st = choose_tensor(d, &use_tc);
@@ -142,14 +163,14 @@ int run_device(DeviceCtx &c, const bf_dims &d, uint8_t *J, const uint8_t *E, con
   }
   TcWeights w;
   plan_weights(w, d.nfrequencies, d.nbeams, d.ndishes);
-  BF_TRY(c.W.reserve(weights_bytes(w)));
-  BF_TRY(c.bias.reserve(bias_bytes(w)));
-  w.W = c.W.as<uint8_t>();
-  w.bias = c.bias.as<float>();
+  BF_TRY(Wb.reserve(weights_bytes(w)));
+  BF_TRY(biasb.reserve(bias_bytes(w)));
+  w.W = Wb.as<uint8_t>();
+  w.bias = biasb.as<float>();
   w.G = G;
   BF_TRY(launch_prep_weights(w, A, s));
   t_last_kernel = "tensor";
-  return to_status(launch_tc(w, d.ntimes, J, E, c.err, s));
+  return to_status(launch_tc(w, d.ntimes, J, E, err, s));
 }
 
 int read_and_clear_err(DeviceCtx &c, cudaStream_t s) {
@@ -162,6 +183,81 @@ int read_and_clear_err(DeviceCtx &c, cudaStream_t s) {
     return BF_ERR_DEVICE_TIMEOUT;
   }
   return BF_OK;
+}
+
+// Times per pipeline chunk of the host-pointer path: about 256 MB of E per
+// chunk (a multiple of 64 times), or all of T when that is one chunk anyway.
+// BF_HOST_CHUNK_BYTES overrides the chunk size (tuning and tests).
+int64_t chunk_times(const bf_dims &d) {
+  const int64_t per_t = std::max<int64_t>(1, d.nfrequencies * d.ndishes * d.npolarizations);
+  int64_t bytes = int64_t(256) << 20;
+  if (const char *env = std::getenv("BF_HOST_CHUNK_BYTES")) bytes = std::max<int64_t>(1, std::atoll(env));
+  int64_t tc = std::max<int64_t>(64, (bytes / per_t) / 64 * 64);
+  return tc * 3 / 2 >= d.ntimes ? d.ntimes : tc;
+}
+
+// Host-pointer pass pipelined over time chunks: E[t0..t1][f][d][p] is
+// contiguous, so each chunk goes in with one copy on one of kLanes streams and
+// is beamformed while the next chunk copies; every chunk writes its times of J
+// (rows of ntimes bytes) in a device buffer that is copied out once at the end.
+// A, G and the tensor-core operand are uploaded / prepared once.  Synchronous;
+// the caller holds c.mu.
+int run_host_pipelined(DeviceCtx &c, const bf_dims &d, uint8_t *J, const uint8_t *E, const uint8_t *A,
+                       const float *G, cudaStream_t caller) {
+  if (!c.lanes_ready) {
+    for (Lane &l : c.lanes) {
+      BF_TRY(cudaStreamCreateWithFlags(&l.s, cudaStreamNonBlocking));
+      BF_TRY(cudaEventCreateWithFlags(&l.done, cudaEventDisableTiming));
+    }
+    c.lanes_ready = true;
+  }
+  bool use_tc = false;
+  int st = choose_tensor(d, &use_tc);
+  if (st != BF_OK) return st;
+  const int64_t T = d.ntimes, per_t = d.nfrequencies * d.ndishes * d.npolarizations;
+  const int64_t tc = chunk_times(d);
+  BF_TRY(c.A.reserve(asize(d)));
+  BF_TRY(c.G.reserve(gsize(d) * sizeof(float)));
+  BF_TRY(c.J.reserve(jsize(d)));
+  Lane &l0 = c.lanes[0];
+  // work already queued on the caller's stream comes first
+  BF_TRY(cudaEventRecord(l0.done, caller));
+  BF_TRY(cudaStreamWaitEvent(l0.s, l0.done, 0));
+  BF_TRY(cudaMemcpyAsync(c.A.p, A, asize(d), cudaMemcpyHostToDevice, l0.s));
+  BF_TRY(cudaMemcpyAsync(c.G.p, G, gsize(d) * sizeof(float), cudaMemcpyHostToDevice, l0.s));
+  TcWeights w;
+  if (use_tc) {
+    plan_weights(w, d.nfrequencies, d.nbeams, d.ndishes);
+    BF_TRY(c.W.reserve(weights_bytes(w)));
+    BF_TRY(c.bias.reserve(bias_bytes(w)));
+    w.W = c.W.as<uint8_t>();
+    w.bias = c.bias.as<float>();
+    w.G = c.G.as<float>();
+    BF_TRY(launch_prep_weights(w, c.A.as<uint8_t>(), l0.s));
+  }
+  BF_TRY(cudaEventRecord(l0.done, l0.s));
+  for (int i = 1; i < kLanes; ++i) BF_TRY(cudaStreamWaitEvent(c.lanes[i].s, l0.done, 0));
+  t_last_kernel = use_tc ? "tensor" : "simt";
+  for (int64_t t0 = 0, k = 0; t0 < T; t0 += tc, ++k) {
+    Lane &l = c.lanes[k % kLanes];
+    const int64_t nt = std::min(tc, T - t0);
+    BF_TRY(l.E.reserve(static_cast<size_t>(nt * per_t)));
+    BF_TRY(cudaMemcpyAsync(l.E.p, E + t0 * per_t, static_cast<size_t>(nt * per_t), cudaMemcpyHostToDevice, l.s));
+    uint8_t *Jc = c.J.as<uint8_t>() + t0;
+    if (use_tc) {
+      BF_TRY(launch_tc(w, nt, Jc, l.E.as<uint8_t>(), c.err, l.s, T));
+    } else {
+      const bf_dims dc{nt, d.nfrequencies, d.ndishes, d.npolarizations, d.nbeams};
+      BF_TRY(launch_simt(dc, Jc, l.E.as<uint8_t>(), c.A.as<uint8_t>(), c.G.as<float>(), l.s, T));
+    }
+  }
+  for (int i = 1; i < kLanes; ++i) {
+    BF_TRY(cudaEventRecord(c.lanes[i].done, c.lanes[i].s));
+    BF_TRY(cudaStreamWaitEvent(l0.s, c.lanes[i].done, 0));
+  }
+  BF_TRY(cudaMemcpyAsync(J, c.J.p, jsize(d), cudaMemcpyDeviceToHost, l0.s));
+  BF_TRY(cudaStreamSynchronize(l0.s));
+  return read_and_clear_err(c, caller);
 }
 
 }  // namespace
@@ -231,7 +327,9 @@ int bf_form_beams_ex(const bf_dims *dims, uint8_t *J, const uint8_t *E, const ui
   std::lock_guard<std::mutex> lk(c->mu);
   if (ptr_kind == BF_PTR_DEVICE) return run_device(*c, d, J, E, A, G, s);
 
-  // Host pointers: stage in, compute, stage out, synchronously (cuda.cu:274-314 does the same around its kernel).
+  // Host pointers: stage in, compute, stage out, synchronously (cuda.cu:274-314 does the same around its
+  // kernel), pipelined over frequency groups when there is more than one.
+  if (chunk_times(d) < d.ntimes) return run_host_pipelined(*c, d, J, E, A, G, s);
   BF_TRY(c->E.reserve(esize(d)));
   BF_TRY(c->A.reserve(asize(d)));
   BF_TRY(c->G.reserve(gsize(d) * sizeof(float)));

@@ -9,9 +9,10 @@
 
 namespace bf {
 
-// Exact integer SIMT kernel (dp4a); any shape with npolarizations <= 2.
+// Exact integer SIMT kernel (dp4a); any shape with npolarizations <= 2.  J
+// rows (b, f, p) are `jpitch` bytes apart (0: ntimes).
 cudaError_t launch_simt(const bf_dims &d, uint8_t *J, const uint8_t *E, const uint8_t *A, const float *G,
-                        cudaStream_t s);
+                        cudaStream_t s, int64_t jpitch = 0);
 
 // Tensor-core path ------------------------------------------------------------
 
@@ -39,7 +40,10 @@ cudaError_t launch_prep_weights(const TcWeights &w, const uint8_t *A, cudaStream
 
 // Beamforms T times of device E into device J with prepared weights.  `err`
 // is a device int that receives a nonzero DeviceError on an expired wait.
-cudaError_t launch_tc(const TcWeights &w, int64_t T, uint8_t *J, const uint8_t *E, int *err, cudaStream_t s);
+// J rows (b, f, p) are `jpitch` bytes apart (0: T), so a time chunk of a longer
+// pass can be written in place: E and J point at the chunk's first time.
+cudaError_t launch_tc(const TcWeights &w, int64_t T, uint8_t *J, const uint8_t *E, int *err, cudaStream_t s,
+                      int64_t jpitch = 0);
 
 // Failure-path test hook: nonzero makes the producer of later tensor-core
 // launches issue nothing, so the kernel's bounded waits expire.

@@ -34,7 +34,7 @@ __device__ __forceinline__ int requant(float g, int raw) {
 __global__ void __launch_bounds__(kThreads) bf_form_beams_simt(uint8_t *__restrict__ J, const uint8_t *__restrict__ E,
                                                                const uint8_t *__restrict__ A,
                                                                const float *__restrict__ G, int64_t T, int64_t F,
-                                                               int64_t D, int64_t P, int64_t B) {
+                                                               int64_t D, int64_t P, int64_t B, int64_t jpitch) {
   __shared__ int32_t s_er[2][kTT][kDQ + 1];
   __shared__ int32_t s_ei[2][kTT][kDQ + 1];
   __shared__ int32_t s_ar[kBB][kDQ];
@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(kThreads) bf_form_beams_simt(uint8_t *__restri
         const int jre = requant(g, acc_re[k]);
         const int jim = requant(g, acc_im[k]);
         // ucomplex4(Jre, Jim) at Jlinear(b,f,p,t) (cpu.cxx:40-41, icomplex4.hxx:33)
-        J[((b * F + f) * P + p) * T + t] =
+        J[((b * F + f) * P + p) * jpitch + t] =
             static_cast<uint8_t>((((static_cast<uint32_t>(jre) & 15u) << 4) | (static_cast<uint32_t>(jim) & 15u)) ^
                                  0x88u);
       }
@@ -139,14 +139,15 @@ __global__ void __launch_bounds__(kThreads) bf_form_beams_simt(uint8_t *__restri
 }  // namespace
 
 cudaError_t launch_simt(const bf_dims &d, uint8_t *J, const uint8_t *E, const uint8_t *A, const float *G,
-                        cudaStream_t s) {
+                        cudaStream_t s, int64_t jpitch) {
+  if (jpitch <= 0) jpitch = d.ntimes;
   if (d.npolarizations < 1 || d.npolarizations > 2) return cudaErrorInvalidValue;
   const int64_t gx = (d.ntimes + kTT - 1) / kTT;
   const int64_t gz = (d.nbeams + kBB - 1) / kBB;
   if (gx > 0x7FFFFFFF || d.nfrequencies > 65535 || gz > 65535) return cudaErrorInvalidConfiguration;
   const dim3 grid(static_cast<unsigned>(gx), static_cast<unsigned>(d.nfrequencies), static_cast<unsigned>(gz));
   bf_form_beams_simt<<<grid, kThreads, 0, s>>>(J, E, A, G, d.ntimes, d.nfrequencies, d.ndishes, d.npolarizations,
-                                               d.nbeams);
+                                               d.nbeams, jpitch);
   return cudaGetLastError();
 }
 

@@ -70,6 +70,7 @@ constexpr int kMaxRaw = 16;
 struct TcParams {
   int T, F, D, B;
   uint8_t *J;
+  int64_t jpitch;  // bytes between consecutive (b, f, p) rows of J (the full ntimes)
   int nb_pass;  // beams per pass
   int npass;
   int ntt;      // time tiles per frequency
@@ -451,7 +452,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             if (b < p.B) {
               // J[b][f][p][t..t+3] (Jlinear, arraysizes.hxx:92)
               uint32_t *dst = reinterpret_cast<uint32_t *>(
-                  p.J + ((static_cast<int64_t>(b) * p.F + f) * 2 + pol) * p.T + t);
+                  p.J + ((static_cast<int64_t>(b) * p.F + f) * 2 + pol) * p.jpitch + t);
               __stcs(dst, w[h2]);
             }
           }
@@ -612,7 +613,8 @@ cudaError_t launch_prep_weights(const TcWeights &w, const uint8_t *A, cudaStream
   return cudaGetLastError();
 }
 
-cudaError_t launch_tc(const TcWeights &w, int64_t T, uint8_t *J, const uint8_t *E, int *err, cudaStream_t s) {
+cudaError_t launch_tc(const TcWeights &w, int64_t T, uint8_t *J, const uint8_t *E, int *err, cudaStream_t s,
+                      int64_t jpitch) {
   const int64_t F = w.F, D = w.D, B = w.B;
   if ((reinterpret_cast<uintptr_t>(E) & 15u) || (reinterpret_cast<uintptr_t>(J) & 15u)) return cudaErrorMisalignedAddress;
   TcParams p{};
@@ -621,6 +623,8 @@ cudaError_t launch_tc(const TcWeights &w, int64_t T, uint8_t *J, const uint8_t *
   p.D = static_cast<int>(D);
   p.B = static_cast<int>(B);
   p.J = J;
+  p.jpitch = jpitch > 0 ? jpitch : T;
+  if (p.jpitch < T || (p.jpitch & 3)) return cudaErrorInvalidValue;
   p.nb_pass = w.nb_pass;
   p.npass = w.npass;
   p.ntt = static_cast<int>((T + kTT - 1) / kTT);

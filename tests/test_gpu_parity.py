@@ -133,6 +133,19 @@ def test_plain_beamform_workload_drop_in(bflib, cuda, golden):
     np.testing.assert_array_equal(J, J2)
 
 
+@pytest.mark.parametrize("shape", [(1000, 3, 512, 2, 96), (400, 5, 30, 2, 17), (1024, 2, 64, 2, 8)])
+def test_host_pointer_pipeline(bflib, cuda, oracle, shape, monkeypatch):
+    """Host-pointer calls pipelined over time chunks on several streams (small
+    chunks forced here; a ragged last chunk; tensor and SIMT shapes); the bytes
+    equal the oracle's."""
+    monkeypatch.setenv("BF_HOST_CHUNK_BYTES", str(64 * 1024))
+    d = bflib.Dims(*shape)
+    E, A, G = bflib.seeded_host_inputs(d, 31)
+    J = np.full(d.jsize, 0x5A, np.uint8)
+    bflib.form_beams_ex(d, J, E, A, G)
+    np.testing.assert_array_equal(J, oracle.form_beams(oracle_dims(oracle, d), E, A, G))
+
+
 def _extreme_inputs(d, kind):
     E = np.empty(d.esize, np.uint8)
     A = np.empty(d.asize, np.uint8)
