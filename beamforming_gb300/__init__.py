@@ -54,6 +54,10 @@ EXPORTED_SYMBOLS = (
     "bf_weights_destroy",
     "bf_form_beams_resident",
     "bf_form_beams_noalloc",
+    "bf_batch_create",
+    "bf_batch_run",
+    "bf_batch_info",
+    "bf_batch_destroy",
     "bf_adler32_device",
     "bf_fill_random_device",
     "bf_fill_random_host",
@@ -154,6 +158,10 @@ def lib() -> ctypes.CDLL:
         L.bf_weights_destroy.argtypes = [vp]
         L.bf_form_beams_resident.argtypes = [vp, ctypes.c_int64, u8p, u8p, vp]
         L.bf_form_beams_noalloc.argtypes = [D, u8p, u8p, u8p, fp, vp]
+        L.bf_batch_create.argtypes = [ctypes.POINTER(vp), ctypes.c_void_p, ctypes.c_int, vp]
+        L.bf_batch_run.argtypes = [vp, vp]
+        L.bf_batch_info.argtypes = [vp] + [ctypes.POINTER(ctypes.c_int)] * 4 + [ctypes.POINTER(ctypes.c_float)]
+        L.bf_batch_destroy.argtypes = [vp]
         L.bf_adler32_device.argtypes = [u8p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_uint32), vp]
         L.bf_fill_random_device.argtypes = [u8p, ctypes.c_size_t, ctypes.c_uint64, ctypes.c_uint64, vp]
         L.bf_fill_random_host.argtypes = [u8p, ctypes.c_size_t, ctypes.c_uint64, ctypes.c_uint64]
@@ -310,6 +318,59 @@ class ResidentWeights:
     def close(self) -> None:
         if getattr(self, "_h", None):
             lib().bf_weights_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class _Problem(ctypes.Structure):
+    _fields_ = [
+        ("weights", ctypes.c_void_p),
+        ("ntimes", ctypes.c_int64),
+        ("E", ctypes.c_void_p),
+        ("J", ctypes.c_void_p),
+    ]
+
+
+class Batch:
+    """Many uneven problems (resident weights, ntimes, device E, device J) run
+    as one persistent launch; the schedule is autotuned at creation and the
+    launch replayed from a CUDA graph by ``run()``."""
+
+    def __init__(self, problems, stream=None):
+        arr = (_Problem * len(problems))()
+        self._keep = []
+        for i, (weights, ntimes, E, J) in enumerate(problems):
+            pe, ke = _ptr(E, np.uint8, ntimes * weights.nfrequencies * weights.ndishes * 2)
+            pj, kj = _ptr(J, np.uint8, weights.nbeams * weights.nfrequencies * 2 * ntimes, writable=True)
+            if ke != PTR_DEVICE or kj != PTR_DEVICE:
+                raise ValueError("batch problems take CUDA tensors")
+            arr[i] = _Problem(weights._h, ntimes, pe, pj)
+            self._keep.append((weights, E, J))
+        h = ctypes.c_void_p()
+        _check(lib().bf_batch_create(ctypes.byref(h), arr, len(problems), _stream_handle(stream)), "bf_batch_create")
+        self._h = h
+
+    def run(self, stream=None) -> None:
+        _check(lib().bf_batch_run(self._h, _stream_handle(stream)), "bf_batch_run")
+
+    def info(self) -> dict:
+        nt, order, ws, raw, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
+        _check(
+            lib().bf_batch_info(self._h, ctypes.byref(nt), ctypes.byref(order), ctypes.byref(ws), ctypes.byref(raw),
+                                ctypes.byref(ms)),
+            "bf_batch_info",
+        )
+        return {"ntiles": nt.value, "order": ("given", "largest_first")[order.value], "wslots": ws.value,
+                "raw_slots": raw.value, "tuned_ms": ms.value}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().bf_batch_destroy(self._h)
             self._h = None
 
     def __del__(self):

@@ -261,16 +261,18 @@ int run_host_pipelined(DeviceCtx &c, const bf_dims &d, uint8_t *J, const uint8_t
 }
 
 }  // namespace
+
+int device_error_word(int **out) {
+  DeviceCtx *c = nullptr;
+  const int st = current_ctx(&c);
+  if (st != BF_OK) return st;
+  *out = c->err;
+  return BF_OK;
+}
+
 }  // namespace bf
 
 using namespace bf;
-
-struct bf_weights {
-  int device = 0;
-  TcWeights tc;
-  uint8_t *A = nullptr;  // raw A kept for the SIMT path
-  float *G = nullptr;
-};
 
 extern "C" {
 

@@ -1,0 +1,196 @@
+// bf_batch.cu -- many uneven beamforming problems in one persistent launch.
+//
+// A batch is a fixed set of problems (each: resident weights for some
+// frequencies, a number of times, device E and J).  Every problem keeps its own
+// shape -- ntimes and nbeams may all differ; ndishes is shared -- and the
+// tensor-core kernel walks one tile list that spans all of them.  At creation
+// an autotuner times a few schedules (tile order x shared-memory ring plan) on
+// the real buffers and keeps the fastest; the chosen launch is then captured
+// in a CUDA graph, and bf_batch_run() replays it.
+#include "bf_internal.h"
+
+#include <algorithm>
+#include <numeric>
+#include <vector>
+
+struct bf_batch {
+  int device = 0;
+  int nprob = 0;
+  int ntiles = 0;
+  int max_nb_pass = 0;
+  int64_t D = 0;
+  int *err = nullptr;
+  bf::TcProblem *table = nullptr;  // device copy, launch order
+  bf::TcRingPlan plan;
+  int order = 0;                   // chosen tile order (0: as given, 1: largest problem first)
+  float tuned_ms = 0.0f;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+using namespace bf;
+
+int status_of(cudaError_t e) {
+  if (e == cudaSuccess) return BF_OK;
+  if (e == cudaErrorMemoryAllocation) return BF_ERR_OUT_OF_MEMORY;
+  return BF_ERR_CUDA;
+}
+
+#define BF_TRY(expr)                               \
+  do {                                             \
+    const cudaError_t e_ = (expr);                 \
+    if (e_ != cudaSuccess) return status_of(e_);   \
+  } while (0)
+
+// Problem records in the given order with tile_begin filled in.
+std::vector<TcProblem> ordered(const std::vector<TcProblem> &probs, const std::vector<int> &order, int *ntiles) {
+  std::vector<TcProblem> out;
+  out.reserve(order.size());
+  int64_t begin = 0;
+  for (int i : order) {
+    TcProblem P = probs[i];
+    P.tile_begin = static_cast<int>(begin);
+    begin += tc_problem_tiles(P);
+    out.push_back(P);
+  }
+  *ntiles = static_cast<int>(begin);
+  return out;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bf_batch_create(bf_batch **out, const bf_problem *problems, int nproblems, bf_stream_t stream) {
+  if (!out || !problems || nproblems <= 0) return BF_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int64_t D = -1;
+  int max_nb = 0;
+  std::vector<TcProblem> probs(static_cast<size_t>(nproblems));
+  for (int i = 0; i < nproblems; ++i) {
+    const bf_problem &q = problems[i];
+    if (!q.weights || !q.E || !q.J || q.ntimes <= 0) return BF_ERR_INVALID_ARGUMENT;
+    const TcWeights &w = q.weights->tc;
+    if (D < 0) D = w.D;
+    const bf_dims d{q.ntimes, w.F, w.D, 2, w.B};
+    if (w.D != D || !tc_supported(d)) return BF_ERR_UNSUPPORTED;
+    if ((reinterpret_cast<uintptr_t>(q.E) | reinterpret_cast<uintptr_t>(q.J)) & 15u) return BF_ERR_UNSUPPORTED;
+    BF_TRY(tc_make_problem(probs[i], w, q.ntimes, q.J, q.E, 0));
+    max_nb = std::max(max_nb, w.nb_pass);
+  }
+  int *err = nullptr;
+  int st = device_error_word(&err);
+  if (st != BF_OK) return st;
+
+  bf_batch *b = new bf_batch();
+  cudaGetDevice(&b->device);
+  b->nprob = nproblems;
+  b->max_nb_pass = max_nb;
+  b->D = D;
+  b->err = err;
+  if (cudaMalloc(&b->table, sizeof(TcProblem) * nproblems) != cudaSuccess) {
+    delete b;
+    return BF_ERR_OUT_OF_MEMORY;
+  }
+
+  // Autotune: tile order x ring plan, each timed on the real buffers (every
+  // candidate writes the same J, so the outputs are valid afterwards).
+  std::vector<int> given(static_cast<size_t>(nproblems));
+  std::iota(given.begin(), given.end(), 0);
+  std::vector<int> largest = given;
+  std::stable_sort(largest.begin(), largest.end(), [&](int x, int y) {
+    return tc_problem_tiles(probs[x]) > tc_problem_tiles(probs[y]);
+  });
+  const std::vector<int> *orders[2] = {&given, &largest};
+  TcRingPlan plans[3];
+  plans[1].wslots = 4;
+  plans[1].raw = 8;
+  plans[2].wslots = 2;
+  plans[2].raw = 12;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = -1.0f;
+  st = BF_OK;
+  for (int o = 0; o < 2 && st == BF_OK; ++o) {
+    int ntiles = 0;
+    const std::vector<TcProblem> table = ordered(probs, *orders[o], &ntiles);
+    cudaError_t e = cudaMemcpyAsync(b->table, table.data(), sizeof(TcProblem) * table.size(),
+                                    cudaMemcpyHostToDevice, s);
+    for (int pl = 0; pl < 3 && e == cudaSuccess; ++pl) {
+      e = launch_tc_grouped(b->table, nproblems, ntiles, D, max_nb, plans[pl], err, s);  // warm-up
+      if (e != cudaSuccess) break;
+      cudaEventRecord(e0, s);
+      for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep)
+        e = launch_tc_grouped(b->table, nproblems, ntiles, D, max_nb, plans[pl], err, s);
+      cudaEventRecord(e1, s);
+      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+      float ms = 0.0f;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+      if (e == cudaSuccess && (best < 0.0f || ms < best)) {
+        best = ms;
+        b->order = o;
+        b->plan = plans[pl];
+        b->ntiles = ntiles;
+      }
+    }
+    if (e != cudaSuccess) st = status_of(e);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st == BF_OK) {
+    int ntiles = 0;
+    const std::vector<TcProblem> table = ordered(probs, *orders[b->order], &ntiles);
+    b->tuned_ms = best / 3.0f;
+    cudaError_t e = cudaMemcpyAsync(b->table, table.data(), sizeof(TcProblem) * table.size(),
+                                    cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    // capture the chosen launch in a graph
+    cudaStream_t cap = nullptr;
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      const cudaError_t le = launch_tc_grouped(b->table, nproblems, ntiles, D, max_nb, b->plan, err, cap);
+      e = cudaStreamEndCapture(cap, &b->graph);
+      if (le != cudaSuccess) e = le;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+    if (cap) cudaStreamDestroy(cap);
+    if (e != cudaSuccess) st = status_of(e);
+  }
+  if (st != BF_OK) {
+    bf_batch_destroy(b);
+    return st;
+  }
+  *out = b;
+  return BF_OK;
+}
+
+int bf_batch_run(bf_batch *b, bf_stream_t stream) {
+  if (!b || !b->exec) return BF_ERR_INVALID_ARGUMENT;
+  return status_of(cudaGraphLaunch(b->exec, static_cast<cudaStream_t>(stream)));
+}
+
+int bf_batch_info(const bf_batch *b, int *ntiles, int *order, int *wslots, int *raw, float *tuned_ms) {
+  if (!b) return BF_ERR_INVALID_ARGUMENT;
+  if (ntiles) *ntiles = b->ntiles;
+  if (order) *order = b->order;
+  if (wslots) *wslots = b->plan.wslots;
+  if (raw) *raw = b->plan.raw;
+  if (tuned_ms) *tuned_ms = b->tuned_ms;
+  return BF_OK;
+}
+
+int bf_batch_destroy(bf_batch *b) {
+  if (!b) return BF_OK;
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  if (b->table) cudaFree(b->table);
+  delete b;
+  return BF_OK;
+}
+
+}  // extern "C"

@@ -2,6 +2,7 @@
 // kernel translation units.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <cstdint>
 
@@ -45,6 +46,42 @@ cudaError_t launch_prep_weights(const TcWeights &w, const uint8_t *A, cudaStream
 cudaError_t launch_tc(const TcWeights &w, int64_t T, uint8_t *J, const uint8_t *E, int *err, cudaStream_t s,
                       int64_t jpitch = 0);
 
+// One beamforming problem of a tensor-core launch: operand descriptors,
+// pointers, shape.  A plain launch carries one inline; a grouped launch reads
+// an array of them from device memory, ordered by tile_begin.
+struct alignas(64) TcProblem {
+  CUtensorMap tm_e;  // E[t][f][d*p] bytes: dims {2D, F, T}, box {128, 1, 64}, 128B swizzle
+  CUtensorMap tm_w;  // W[f][n][k] bytes: dims {2D, nw, F}, box {128, 2*nb_pass, 1}, 128B swizzle
+  uint8_t *J;
+  const float *G;
+  const float *bias;
+  int64_t jpitch;    // bytes between consecutive (b, f, p) rows of J
+  int T, F, B;
+  int nb_pass;       // beams per pass
+  int npass;
+  int ntt;           // time tiles per frequency
+  int nw_pad;        // bias entries per frequency
+  int tile_begin;    // first tile of this problem in the launch
+};
+
+// Shared-memory ring depths of a launch (0: planner default).
+struct TcRingPlan {
+  int wslots = 0;
+  int raw = 0;
+};
+
+// Fills a problem record (tile_begin left 0) for T times of E with weights w.
+cudaError_t tc_make_problem(TcProblem &P, const TcWeights &w, int64_t T, uint8_t *J, const uint8_t *E,
+                            int64_t jpitch);
+// Tiles of a problem, and K stages per tile for D dishes.
+int64_t tc_problem_tiles(const TcProblem &P);
+int tc_stages_per_tile(int64_t D);
+
+// One persistent launch over nprob problems (records in device memory; all
+// with D dishes).  max_nb_pass = the largest nb_pass among them.
+cudaError_t launch_tc_grouped(const TcProblem *table, int nprob, int ntiles, int64_t D, int max_nb_pass,
+                              const TcRingPlan &plan, int *err, cudaStream_t s);
+
 // Failure-path test hook: nonzero makes the producer of later tensor-core
 // launches issue nothing, so the kernel's bounded waits expire.
 void tc_set_test_stall(int on);
@@ -63,4 +100,17 @@ cudaError_t launch_adler_combine(const uint32_t *partials, size_t len, uint32_t 
 // Workload generator.
 cudaError_t launch_fill_random(uint8_t *dst, size_t n, uint64_t seed, uint64_t stream_id, cudaStream_t s);
 
+}  // namespace bf
+
+// Device-resident beam weights behind the C ABI's opaque bf_weights handle.
+struct bf_weights {
+  int device = 0;
+  bf::TcWeights tc;
+  uint8_t *A = nullptr;  // raw A kept for the SIMT path
+  float *G = nullptr;
+};
+
+namespace bf {
+// The calling thread's device error word (allocated on first use).
+int device_error_word(int **out);
 }  // namespace bf

@@ -41,6 +41,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cstring>
 #include <cudaTypedefs.h>
 
 namespace bf {
@@ -67,24 +68,37 @@ constexpr int kMaxWSlots = 6;
 constexpr int kMinRaw = 4;
 constexpr int kMaxRaw = 16;
 
+
 struct TcParams {
-  int T, F, D, B;
-  uint8_t *J;
-  int64_t jpitch;  // bytes between consecutive (b, f, p) rows of J (the full ntimes)
-  int nb_pass;  // beams per pass
-  int npass;
-  int ntt;      // time tiles per frequency
-  int nk;       // K stages per tile
+  TcProblem one;            // the problem of a plain launch
+  const TcProblem *table;   // grouped launch: nprob problems in device memory, by tile_begin
+  int nprob;
   int ntiles;
-  int stages;   // unpacked-operand stages in TMEM
-  int wslots;   // W slots in smem
-  int raw;      // raw E slots in smem
-  int nw_pad;
-  int test_stall;  // nonzero: the producers issue nothing (failure-path test)
-  const float *G;
-  const float *bias;
+  int nk;                   // K stages per tile (every problem has the same dishes)
+  int max_nb_pass;          // sizes the W slots, gain buffers and TMEM layout
+  int stages;               // unpacked-operand stages in TMEM
+  int wslots;               // W slots in smem
+  int raw;                  // raw E slots in smem
+  int test_stall;           // nonzero: the producers issue nothing (failure-path test)
   int *err;
 };
+
+// Problem of a tile and the tile's index inside it.
+template <bool kGrouped>
+__device__ __forceinline__ const TcProblem &problem_of(const TcParams &p, int tile, int &lt) {
+  if constexpr (!kGrouped) {
+    lt = tile;
+    return p.one;
+  } else {
+    int lo = 0, hi = p.nprob - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (p.table[mid].tile_begin <= tile) lo = mid; else hi = mid - 1;
+    }
+    lt = tile - p.table[lo].tile_begin;
+    return p.table[lo];
+  }
+}
 
 struct SmemPlan {
   int wbox, wbytes;
@@ -135,13 +149,12 @@ __device__ __forceinline__ uint32_t sw128_offset(uint32_t r, uint32_t j) {
   return (r >> 3) * 1024u + (r & 7u) * 128u + ((j ^ (r & 7u)) << 4);
 }
 
-__global__ void __launch_bounds__(kThreads, 1)
-    bf_form_beams_tc(const __grid_constant__ CUtensorMap tm_e, const __grid_constant__ CUtensorMap tm_w,
-                     const TcParams p) {
+template <bool kGrouped>
+__global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_constant__ TcParams p) {
   extern __shared__ uint8_t smem_dyn[];
   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_dyn) + 1023) & ~uintptr_t(1023));
   const int S = p.stages, SW = p.wslots, R = p.raw;
-  const SmemPlan sp = smem_plan(S, SW, R, p.nb_pass);
+  const SmemPlan sp = smem_plan(S, SW, R, p.max_nb_pass);
   uint8_t *sW = smem + sp.off_w;
   uint8_t *sR = smem + sp.off_r;
   float *sG = reinterpret_cast<float *>(smem + sp.off_g);
@@ -158,7 +171,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
-  const int ncols = 2 * p.nb_pass;                     // accumulator columns (GEMM N)
+  const int ncols = 2 * p.max_nb_pass;                 // accumulator columns reserved (largest GEMM N)
   const int per_half = (kAccCols - ncols) / kStageCols;  // unpacked stages beside each accumulator
 
   if (threadIdx.x == 0) {
@@ -184,9 +197,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     tmem_alloc(smem_u32(tmem_holder), 2 * kAccCols);
     tmem_relinquish();
   }
-  if (warp == kEProdWarp && lane == 0) {
-    tma_prefetch_desc(&tm_e);
-    tma_prefetch_desc(&tm_w);
+  if (!kGrouped && warp == kEProdWarp && lane == 0) {
+    tma_prefetch_desc(&p.one.tm_e);
+    tma_prefetch_desc(&p.one.tm_w);
   }
   tc_fence_before();
   __syncthreads();
@@ -202,8 +215,10 @@ __global__ void __launch_bounds__(kThreads, 1)
       uint32_t issued = 0;
       bool ok = true;
       for (int tile = blockIdx.x; ok && tile < p.ntiles; tile += gridDim.x) {
-        const int tt = (tile / p.npass) % p.ntt;
-        const int f = tile / (p.npass * p.ntt);
+        int lt;
+        const TcProblem &P = problem_of<kGrouped>(p, tile, lt);
+        const int tt = (lt / P.npass) % P.ntt;
+        const int f = lt / (P.npass * P.ntt);
         for (int ks = 0; ks < p.nk; ++ks, rr.advance(), ++issued) {
           const int r = static_cast<int>(rr.idx);
           if (!mbar_wait(raw_empty(r), rr.phase ^ 1u, err, kDevTimeoutEmpty)) {
@@ -213,7 +228,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           mbar_arrive_expect_tx(raw_full(r), kRawBytes);
 #pragma unroll
           for (int h = 0; h < kSub; ++h)
-            tma_load_3d(smem_u32(sR + r * kRawBytes + h * kRawBox), &tm_e, raw_full(r), (ks * kSub + h) * kKC, f,
+            tma_load_3d(smem_u32(sR + r * kRawBytes + h * kRawBox), &P.tm_e, raw_full(r), (ks * kSub + h) * kKC, f,
                         tt * kTT, pol_e);
         }
       }
@@ -230,19 +245,22 @@ __global__ void __launch_bounds__(kThreads, 1)
       uint32_t it = 0;
       bool ok = true;
       for (int tile = blockIdx.x; ok && tile < p.ntiles; tile += gridDim.x) {
-        const int pass = tile % p.npass;
-        const int f = tile / (p.npass * p.ntt);
+        int lt;
+        const TcProblem &P = problem_of<kGrouped>(p, tile, lt);
+        const int pass = lt % P.npass;
+        const int f = lt / (P.npass * P.ntt);
+        const int wbox = 2 * P.nb_pass * kKC;
         for (int ks = 0; ks < p.nk; ++ks, ++it, wr.advance()) {
           const int s = static_cast<int>(wr.idx);
           if (!mbar_wait(w_empty(s), wr.phase ^ 1u, err, kDevTimeoutEmpty)) {
             ok = false;
             break;
           }
-          mbar_arrive_expect_tx(w_full(s), sp.wbytes);
+          mbar_arrive_expect_tx(w_full(s), kSub * wbox);
 #pragma unroll
           for (int h = 0; h < kSub; ++h)
-            tma_load_3d(smem_u32(sW + s * sp.wbytes + h * sp.wbox), &tm_w, w_full(s), (ks * kSub + h) * kKC,
-                        pass * 2 * p.nb_pass, f, pol_w);
+            tma_load_3d(smem_u32(sW + s * sp.wbytes + h * wbox), &P.tm_w, w_full(s), (ks * kSub + h) * kKC,
+                        pass * 2 * P.nb_pass, f, pol_w);
         }
       }
       if (!ok) {
@@ -253,11 +271,14 @@ __global__ void __launch_bounds__(kThreads, 1)
   } else if (warp == kMmaWarp) {
     // ------------------------------------------------------------ MMA issuer
     if (lane == 0) {
-      const uint32_t idesc = idesc_e4m3_f32(kBM, ncols);
       Ring ar(S), wr(SW);
       uint32_t local = 0;
       bool ok = true;
       for (int tile = blockIdx.x; ok && tile < p.ntiles; tile += gridDim.x, ++local) {
+        int lt;
+        const TcProblem &P = problem_of<kGrouped>(p, tile, lt);
+        const uint32_t idesc = idesc_e4m3_f32(kBM, 2 * P.nb_pass);
+        const int wbox = 2 * P.nb_pass * kKC;
         const uint32_t ab = local & 1u;
         const uint32_t aph = (local >> 1) & 1u;
         if (!mbar_wait(accempty(ab), aph ^ 1u, err, kDevTimeoutAccEmpty)) break;
@@ -277,7 +298,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
           for (int kk = 0; kk < kStageK / 32; ++kk) {
             // K step kk: box kk / 4, 32 bytes into its 128-byte rows (descriptor address field is in 16 B units)
-            const uint64_t off = static_cast<uint64_t>(((kk >> 2) * sp.wbox + 32 * (kk & 3)) >> 4);
+            const uint64_t off = static_cast<uint64_t>(((kk >> 2) * wbox + 32 * (kk & 3)) >> 4);
             mma_f8f6f4_ts(d_tmem, a_tmem + 8 * kk, b_desc + off, idesc, (ks | kk) != 0 ? 1u : 0u);
           }
           mma_commit(empty(s));
@@ -366,33 +387,38 @@ __global__ void __launch_bounds__(kThreads, 1)
     // byte-transpose selectors: 4 lanes x 4 beams -> each lane holds one beam's 4 times
     const uint32_t sel1 = (j4 & 1) ? 0x3715u : 0x6240u;
     const uint32_t sel2 = (j4 & 2) ? 0x3276u : 0x5410u;
-    const int nchunk = p.nb_pass / 8;
-    const int c_mid = (nchunk + 1) / 2;
-    const int c_begin = half ? c_mid : 0, c_end = half ? nchunk : c_mid;
-    const int ng = 3 * p.nb_pass;  // floats per gain buffer
+    const int gstride = 3 * p.max_nb_pass;  // floats per gain buffer
     const float kMagic = 12582920.0f;  // 1.5 * 2^23 + 8: x + kMagic has rint(x) + 8 in its low mantissa bits
 
-    // gains and row sums of one (frequency, beam pass): value i of the buffer
+    // gains [nb_pass] and row sums [2 * nb_pass] of a tile's (frequency, beam pass): value i
     auto gain_value = [&](int tile, int i) -> float {
-      const int pass = tile % p.npass;
-      const int f = tile / (p.npass * p.ntt);
-      const int b0 = pass * p.nb_pass;
-      if (i < p.nb_pass) return (b0 + i < p.B) ? __ldg(p.G + static_cast<int64_t>(f) * p.B + b0 + i) : 0.0f;
-      return __ldg(p.bias + static_cast<int64_t>(f) * p.nw_pad + 2 * b0 + (i - p.nb_pass));
+      int lt;
+      const TcProblem &Q = problem_of<kGrouped>(p, tile, lt);
+      if (i >= 3 * Q.nb_pass) return 0.0f;
+      const int pass = lt % Q.npass;
+      const int f = lt / (Q.npass * Q.ntt);
+      const int b0 = pass * Q.nb_pass;
+      if (i < Q.nb_pass) return (b0 + i < Q.B) ? __ldg(Q.G + static_cast<int64_t>(f) * Q.B + b0 + i) : 0.0f;
+      return __ldg(Q.bias + static_cast<int64_t>(f) * Q.nw_pad + 2 * b0 + (i - Q.nb_pass));
     };
     if (static_cast<int>(blockIdx.x) < p.ntiles)
-      for (int i = threadIdx.x; i < ng; i += kEpiThreads) sG[i] = gain_value(blockIdx.x, i);
+      for (int i = threadIdx.x; i < gstride; i += kEpiThreads) sG[i] = gain_value(blockIdx.x, i);
 
     uint32_t local = 0;
     for (int tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x, ++local) {
-      const int pass = tile % p.npass;
-      const int tt = (tile / p.npass) % p.ntt;
-      const int f = tile / (p.npass * p.ntt);
+      int lt;
+      const TcProblem &P = problem_of<kGrouped>(p, tile, lt);
+      const int pass = lt % P.npass;
+      const int tt = (lt / P.npass) % P.ntt;
+      const int f = lt / (P.npass * P.ntt);
+      const int nchunk = P.nb_pass / 8;
+      const int c_mid = (nchunk + 1) / 2;
+      const int c_begin = half ? c_mid : 0, c_end = half ? nchunk : c_mid;
       const uint32_t ab = local & 1u;
       const uint32_t aph = (local >> 1) & 1u;
-      const int b0 = pass * p.nb_pass;
-      const float *gcur = sG + (local & 1u) * ng;
-      float *gnext = sG + ((local + 1) & 1u) * ng;
+      const int b0 = pass * P.nb_pass;
+      const float *gcur = sG + (local & 1u) * gstride;
+      float *gnext = sG + ((local + 1) & 1u) * gstride;
       named_bar_sync(1, kEpiThreads);  // this tile's gains are written; last tile's readers are done
       // next tile's gains: loads in flight during this tile, stored at its end
       const int next = tile + static_cast<int>(gridDim.x);
@@ -400,19 +426,19 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
       for (int k = 0; k < 2; ++k) {
         const int i = static_cast<int>(threadIdx.x) + k * kEpiThreads;
-        if (next < p.ntiles && i < ng) pre[k] = gain_value(next, i);
+        if (next < p.ntiles && i < gstride) pre[k] = gain_value(next, i);
       }
       const bool got = mbar_wait(accfull(ab), aph, err, kDevTimeoutAccFull);
       if (!named_bar_and(2, kEpiThreads, got)) break;  // all eight warps leave together
       tc_fence_after();
       const int64_t t = static_cast<int64_t>(tt) * kTT + 16 * q + 4 * g4;  // first of this lane's 4 times
-      const bool t_ok = t < p.T;
+      const bool t_ok = t < P.T;
       const uint32_t acc_addr = tmem_base + ab * kAccCols + lane_addr;
 
       auto process = [&](int c, const uint32_t (&r)[16]) {
         const float4 ga = *reinterpret_cast<const float4 *>(gcur + 8 * c);
         const float4 gb = *reinterpret_cast<const float4 *>(gcur + 8 * c + 4);
-        const float *bs = gcur + p.nb_pass + 16 * c;
+        const float *bs = gcur + P.nb_pass + 16 * c;
         const float4 bra = *reinterpret_cast<const float4 *>(bs);
         const float4 brb = *reinterpret_cast<const float4 *>(bs + 4);
         const float4 bia = *reinterpret_cast<const float4 *>(bs + 8);
@@ -449,10 +475,10 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
           for (int h2 = 0; h2 < 2; ++h2) {
             const int b = b0 + 8 * c + 4 * h2 + static_cast<int>(j4);
-            if (b < p.B) {
+            if (b < P.B) {
               // J[b][f][p][t..t+3] (Jlinear, arraysizes.hxx:92)
               uint32_t *dst = reinterpret_cast<uint32_t *>(
-                  p.J + ((static_cast<int64_t>(b) * p.F + f) * 2 + pol) * p.jpitch + t);
+                  P.J + ((static_cast<int64_t>(b) * P.F + f) * 2 + pol) * P.jpitch + t);
               __stcs(dst, w[h2]);
             }
           }
@@ -481,7 +507,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
       for (int k = 0; k < 2; ++k) {
         const int i = static_cast<int>(threadIdx.x) + k * kEpiThreads;
-        if (next < p.ntiles && i < ng) gnext[i] = pre[k];
+        if (next < p.ntiles && i < gstride) gnext[i] = pre[k];
       }
     }
   }
@@ -613,75 +639,123 @@ cudaError_t launch_prep_weights(const TcWeights &w, const uint8_t *A, cudaStream
   return cudaGetLastError();
 }
 
-cudaError_t launch_tc(const TcWeights &w, int64_t T, uint8_t *J, const uint8_t *E, int *err, cudaStream_t s,
-                      int64_t jpitch) {
-  const int64_t F = w.F, D = w.D, B = w.B;
+// Fills a problem record: shape, pointers and the two tensor maps.
+static cudaError_t make_problem(TcProblem &P, const TcWeights &w, int64_t T, uint8_t *J, const uint8_t *E,
+                                int64_t jpitch) {
+  const int64_t F = w.F, D = w.D;
   if ((reinterpret_cast<uintptr_t>(E) & 15u) || (reinterpret_cast<uintptr_t>(J) & 15u)) return cudaErrorMisalignedAddress;
-  TcParams p{};
-  p.T = static_cast<int>(T);
-  p.F = static_cast<int>(F);
-  p.D = static_cast<int>(D);
-  p.B = static_cast<int>(B);
-  p.J = J;
-  p.jpitch = jpitch > 0 ? jpitch : T;
-  if (p.jpitch < T || (p.jpitch & 3)) return cudaErrorInvalidValue;
-  p.nb_pass = w.nb_pass;
-  p.npass = w.npass;
-  p.ntt = static_cast<int>((T + kTT - 1) / kTT);
-  p.nk = static_cast<int>((D + kStageK / 2 - 1) / (kStageK / 2));
-  const int64_t ntiles = static_cast<int64_t>(p.ntt) * F * p.npass;
-  if (ntiles > 0x7FFFFFFF) return cudaErrorInvalidValue;
-  p.ntiles = static_cast<int>(ntiles);
-  p.nw_pad = w.nw_pad;
-  p.G = w.G;
-  p.bias = w.bias;
-  p.err = err;
-  p.test_stall = g_test_stall;
-  // unpacked stages live in the TMEM columns beside the two accumulators; raw E
-  // slots take the shared memory the W slots leave
-  const int per_half = (kAccCols - 2 * w.nb_pass) / kStageCols;
-  const int stages = std::min(kMaxStages, 2 * per_half);
-  if (stages < 2) return cudaErrorInvalidValue;
-  // shared memory: W slots first (their loads gate the MMA), then raw E slots
-  int wslots = g_plan_wslots > 0 ? g_plan_wslots : kMaxWSlots;
-  int raw = g_plan_raw > 0 ? g_plan_raw : kMinRaw;
-  while (wslots > 2 && smem_plan(stages, wslots, raw, w.nb_pass).total + 1024 > kSmemLimit) --wslots;
-  while (raw < kMaxRaw && smem_plan(stages, wslots, raw + 1, w.nb_pass).total + 1024 <= kSmemLimit &&
-         g_plan_raw <= 0)
-    ++raw;
-  while (raw > 2 && smem_plan(stages, wslots, raw, w.nb_pass).total + 1024 > kSmemLimit) --raw;
-  p.stages = stages;
-  p.wslots = wslots;
-  p.raw = raw;
-  const int smem_bytes = smem_plan(stages, wslots, raw, w.nb_pass).total + 1024;
-  if (smem_bytes > kSmemLimit) return cudaErrorInvalidValue;
-
-  CUtensorMap tm_e, tm_w;
+  std::memset(&P, 0, sizeof(P));
+  P.T = static_cast<int>(T);
+  P.F = static_cast<int>(F);
+  P.B = static_cast<int>(w.B);
+  P.J = J;
+  P.jpitch = jpitch > 0 ? jpitch : T;
+  if (P.jpitch < T || (P.jpitch & 3)) return cudaErrorInvalidValue;
+  P.nb_pass = w.nb_pass;
+  P.npass = w.npass;
+  P.ntt = static_cast<int>((T + kTT - 1) / kTT);
+  P.nw_pad = w.nw_pad;
+  P.G = w.G;
+  P.bias = w.bias;
   {  // E[t][f][d*p] bytes: dims {2D, F, T}
     const cuuint64_t dims[3] = {static_cast<cuuint64_t>(2 * D), static_cast<cuuint64_t>(F),
                                 static_cast<cuuint64_t>(T)};
     const cuuint64_t str[2] = {static_cast<cuuint64_t>(2 * D), static_cast<cuuint64_t>(2 * D * F)};
     const cuuint32_t box[3] = {static_cast<cuuint32_t>(kKC), 1, static_cast<cuuint32_t>(kTT)};
-    if (!make_map(&tm_e, E, 3, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B)) return cudaErrorInvalidValue;
+    if (!make_map(&P.tm_e, E, 3, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B)) return cudaErrorInvalidValue;
   }
   {  // W[f][n][k] bytes: dims {2D, nw, F}
     const cuuint64_t dims[3] = {static_cast<cuuint64_t>(2 * D), static_cast<cuuint64_t>(w.nw),
                                 static_cast<cuuint64_t>(F)};
     const cuuint64_t str[2] = {static_cast<cuuint64_t>(2 * D), static_cast<cuuint64_t>(2 * D * w.nw)};
     const cuuint32_t box[3] = {static_cast<cuuint32_t>(kKC), static_cast<cuuint32_t>(2 * w.nb_pass), 1};
-    if (!make_map(&tm_w, w.W, 3, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B)) return cudaErrorInvalidValue;
+    if (!make_map(&P.tm_w, w.W, 3, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B)) return cudaErrorInvalidValue;
   }
+  return cudaSuccess;
+}
+
+// Ring depths and shared memory for a launch whose largest pass has max_nb_pass beams.
+static cudaError_t plan_launch(TcParams &p, int max_nb_pass, int *smem_bytes) {
+  // unpacked stages live in the TMEM columns beside the two accumulators; raw E
+  // slots take the shared memory the W slots leave
+  const int per_half = (kAccCols - 2 * max_nb_pass) / kStageCols;
+  const int stages = std::min(kMaxStages, 2 * per_half);
+  if (stages < 2) return cudaErrorInvalidValue;
+  // shared memory: W slots first (their loads gate the MMA), then raw E slots
+  int wslots = g_plan_wslots > 0 ? g_plan_wslots : kMaxWSlots;
+  int raw = g_plan_raw > 0 ? g_plan_raw : kMinRaw;
+  while (wslots > 2 && smem_plan(stages, wslots, raw, max_nb_pass).total + 1024 > kSmemLimit) --wslots;
+  while (raw < kMaxRaw && smem_plan(stages, wslots, raw + 1, max_nb_pass).total + 1024 <= kSmemLimit &&
+         g_plan_raw <= 0)
+    ++raw;
+  while (raw > 2 && smem_plan(stages, wslots, raw, max_nb_pass).total + 1024 > kSmemLimit) --raw;
+  p.max_nb_pass = max_nb_pass;
+  p.stages = stages;
+  p.wslots = wslots;
+  p.raw = raw;
+  p.test_stall = g_test_stall;
+  *smem_bytes = smem_plan(stages, wslots, raw, max_nb_pass).total + 1024;
+  return *smem_bytes > kSmemLimit ? cudaErrorInvalidValue : cudaSuccess;
+}
+
+template <bool kGrouped>
+static cudaError_t launch_kernel(const TcParams &p, int smem_bytes, cudaStream_t s) {
   static bool attr_set = false;
   if (!attr_set) {
     const cudaError_t e =
-        cudaFuncSetAttribute(bf_form_beams_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
+        cudaFuncSetAttribute(bf_form_beams_tc<kGrouped>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
-  const int grid = static_cast<int>(std::min<int64_t>(ntiles, num_sms()));
+  const int grid = std::min(p.ntiles, num_sms());
   if (grid <= 0) return cudaSuccess;
-  bf_form_beams_tc<<<grid, kThreads, smem_bytes, s>>>(tm_e, tm_w, p);
+  bf_form_beams_tc<kGrouped><<<grid, kThreads, smem_bytes, s>>>(p);
   return cudaGetLastError();
+}
+
+cudaError_t tc_make_problem(TcProblem &P, const TcWeights &w, int64_t T, uint8_t *J, const uint8_t *E,
+                            int64_t jpitch) {
+  return make_problem(P, w, T, J, E, jpitch);
+}
+
+int64_t tc_problem_tiles(const TcProblem &P) { return static_cast<int64_t>(P.ntt) * P.F * P.npass; }
+
+int tc_stages_per_tile(int64_t D) { return static_cast<int>((D + kStageK / 2 - 1) / (kStageK / 2)); }
+
+cudaError_t launch_tc_grouped(const TcProblem *table, int nprob, int ntiles, int64_t D, int max_nb_pass,
+                              const TcRingPlan &plan, int *err, cudaStream_t s) {
+  TcParams p{};
+  p.table = table;
+  p.nprob = nprob;
+  p.ntiles = ntiles;
+  p.nk = tc_stages_per_tile(D);
+  p.err = err;
+  const int save_w = g_plan_wslots, save_r = g_plan_raw;
+  if (plan.wslots > 0) g_plan_wslots = plan.wslots;
+  if (plan.raw > 0) g_plan_raw = plan.raw;
+  int smem_bytes = 0;
+  const cudaError_t e = plan_launch(p, max_nb_pass, &smem_bytes);
+  g_plan_wslots = save_w;
+  g_plan_raw = save_r;
+  if (e != cudaSuccess) return e;
+  return launch_kernel<true>(p, smem_bytes, s);
+}
+
+cudaError_t launch_tc(const TcWeights &w, int64_t T, uint8_t *J, const uint8_t *E, int *err, cudaStream_t s,
+                      int64_t jpitch) {
+  TcParams p{};
+  cudaError_t e = make_problem(p.one, w, T, J, E, jpitch);
+  if (e != cudaSuccess) return e;
+  const int64_t ntiles = static_cast<int64_t>(p.one.ntt) * w.F * w.npass;
+  if (ntiles > 0x7FFFFFFF) return cudaErrorInvalidValue;
+  p.ntiles = static_cast<int>(ntiles);
+  p.nprob = 1;
+  p.nk = tc_stages_per_tile(w.D);
+  p.err = err;
+  int smem_bytes = 0;
+  e = plan_launch(p, w.nb_pass, &smem_bytes);
+  if (e != cudaSuccess) return e;
+  return launch_kernel<false>(p, smem_bytes, s);
 }
 
 }  // namespace bf

@@ -138,6 +138,39 @@ BF_API int bf_weights_destroy(bf_weights *w);
  * weights; asynchronous on `stream`. */
 BF_API int bf_form_beams_resident(const bf_weights *w, int64_t ntimes, uint8_t *J, const uint8_t *E, bf_stream_t stream);
 
+/* ---------------------------------------------------------------- batches */
+
+/* A fixed set of beamforming problems run as one persistent launch.  No
+ * counterpart in the reference, which runs one compile-time shape per program;
+ * this is the grouped form of bf_form_beams_resident(). */
+typedef struct bf_batch bf_batch;
+
+/* One problem of a batch: ntimes samples of device E[t][f][d][p] beamformed
+ * with resident weights into device J[b][f][p][t].  ntimes, frequencies and
+ * beams may differ between problems; ndishes must be the same for all. */
+typedef struct bf_problem {
+  const bf_weights *weights;
+  int64_t ntimes;
+  const uint8_t *E;
+  uint8_t *J;
+} bf_problem;
+
+/* Builds a batch: times a few launch schedules on the given buffers (tile
+ * order x shared-memory ring plan), keeps the fastest and captures it in a
+ * CUDA graph.  The buffers must stay allocated while the batch exists; their
+ * contents may change between runs.  Each problem needs the tensor-core shape
+ * rules (ntimes % 16 == 0, ndishes % 8 == 0, 16-byte aligned E and J). */
+BF_API int bf_batch_create(bf_batch **out, const bf_problem *problems, int nproblems, bf_stream_t stream);
+
+/* Runs every problem of the batch once (graph replay); asynchronous on `stream`. */
+BF_API int bf_batch_run(bf_batch *batch, bf_stream_t stream);
+
+/* The schedule the autotuner chose: tiles, tile order (0 as given, 1 largest
+ * problem first), ring plan (0 = default) and the tuned time of one run. */
+BF_API int bf_batch_info(const bf_batch *batch, int *ntiles, int *order, int *wslots, int *raw, float *tuned_ms);
+
+BF_API int bf_batch_destroy(bf_batch *batch);
+
 /* ------------------------------------------------------- no allocation */
 
 /* No counterpart in the reference.  For callers that cannot allocate device

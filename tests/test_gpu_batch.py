@@ -1,0 +1,78 @@
+"""Batched uneven problems in one persistent launch: every problem's J equals
+the oracle's and the per-problem launch's, alone and in the mix."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _problem(bf, torch, T, F, D, B, seed):
+    d = bf.Dims(T, F, D, 2, B)
+    E = np.empty(d.esize, np.uint8)
+    A = np.empty(d.asize, np.uint8)
+    bf.fill_random_host(E, seed, 0)
+    bf.fill_random_host(A, seed, 1)
+    G = bf.gains(d)
+    W = bf.ResidentWeights(F, B, D, A, G)
+    Ed = torch.from_numpy(E).cuda()
+    Jd = torch.full((d.jsize,), 0x5A, dtype=torch.uint8, device="cuda")
+    return d, (E, A, G), W, Ed, Jd
+
+
+def _oracle(oracle, d, E, A, G):
+    return oracle.form_beams(oracle.Dims(d.ntimes, d.nfrequencies, d.ndishes, 2, d.nbeams), E, A, G)
+
+
+def test_batch_uneven_shapes(bflib, cuda, oracle):
+    rng = np.random.default_rng(2)
+    shapes = []
+    for i in range(12):
+        T = int(rng.choice([16, 48, 64, 208, 512, 1024, 1296]))
+        B = int(rng.choice([8, 16, 40, 64, 96, 128, 200]))
+        F = int(rng.choice([1, 1, 2]))
+        shapes.append((T, F, 512, B))
+    probs = [_problem(bflib, cuda, T, F, D, B, 100 + i) for i, (T, F, D, B) in enumerate(shapes)]
+    batch = bflib.Batch([(W, d.ntimes, Ed, Jd) for d, _, W, Ed, Jd in probs])
+    info = batch.info()
+    assert info["ntiles"] > 0
+    batch.run()
+    bflib.stream_status()
+    for d, (E, A, G), W, Ed, Jd in probs:
+        np.testing.assert_array_equal(Jd.cpu().numpy(), _oracle(oracle, d, E, A, G), err_msg=str(d))
+    # the same problem alone through the per-problem launch gives the same bytes
+    d, (E, A, G), W, Ed, Jd = probs[3]
+    J1 = cuda.empty_like(Jd)
+    W.form_beams(J1, Ed, d.ntimes)
+    bflib.stream_status()
+    assert cuda.equal(J1, Jd)
+    batch.close()
+
+
+def test_batch_replay_sees_new_inputs(bflib, cuda, oracle):
+    """The captured graph reads the problems' buffers on every run."""
+    probs = [_problem(bflib, cuda, T, 1, 512, B, 7 + T) for T, B in [(256, 96), (64, 16), (512, 128)]]
+    batch = bflib.Batch([(W, d.ntimes, Ed, Jd) for d, _, W, Ed, Jd in probs])
+    for rep in range(2):
+        for k, (d, (E, A, G), W, Ed, Jd) in enumerate(probs):
+            E2 = np.empty_like(E)
+            bflib.fill_random_host(E2, 1000 + 10 * rep + k, 0)
+            Ed.copy_(cuda.from_numpy(E2))
+            probs[k] = (d, (E2, A, G), W, Ed, Jd)
+        batch.run()
+        bflib.stream_status()
+        for d, (E, A, G), W, Ed, Jd in probs:
+            np.testing.assert_array_equal(Jd.cpu().numpy(), _oracle(oracle, d, E, A, G))
+    batch.close()
+
+
+def test_batch_rejects_mixed_dishes_and_odd_times(bflib, cuda):
+    a = _problem(bflib, cuda, 64, 1, 512, 16, 1)
+    b = _problem(bflib, cuda, 64, 1, 256, 16, 2)
+    with pytest.raises(bflib.BeamformError) as ei:
+        bflib.Batch([(x[2], x[0].ntimes, x[3], x[4]) for x in (a, b)])
+    assert ei.value.status == bflib.ERR_UNSUPPORTED
+    c = _problem(bflib, cuda, 40, 1, 512, 16, 3)
+    with pytest.raises(bflib.BeamformError):
+        bflib.Batch([(c[2], 40, c[3], c[4])])
