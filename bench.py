@@ -53,6 +53,12 @@ def parse_args():
         help="only launch the tensor-core kernel (resident weights), for ncu captures; prints no measurement",
     )
     ap.add_argument("--frequencies", type=int, default=None, help="override f (profiling a smaller case)")
+    ap.add_argument(
+        "--workload",
+        choices=["chunk", "batched"],
+        default="chunk",
+        help="chunk: the full single-GPU chunk (default); batched: 128 uneven problems in one persistent launch",
+    )
     return ap.parse_args()
 
 
@@ -419,8 +425,106 @@ def profile_kernel(args):
     print(json.dumps({"profile_kernel": True, "dims": d.__dict__, "adler32_J": hex(bf.adler32_device(J))}))
 
 
+BATCH_NAME = ("128 problems, f=1 d=512 p=2 each, t log-uniform in [512, 32768] rounded to 256, "
+              "b in {16, 32, 64, 96, 128}, seed 2")
+
+
+def batched_problems(seed=2, n=128):
+    """Shapes of the batched workload: t log-uniform over [512, 32768] rounded to
+    a multiple of 256, b drawn from {16, 32, 64, 96, 128}, f = 1, d = 512."""
+    rng = np.random.default_rng(seed)
+    ts = np.exp(rng.uniform(np.log(512), np.log(32768), n))
+    ts = np.clip(np.round(ts / 256).astype(int) * 256, 512, 32768)
+    bs = rng.choice([16, 32, 64, 96, 128], n)
+    return [(int(t), 1, 512, int(b)) for t, b in zip(ts, bs)]
+
+
+def run_batched(args):
+    """One persistent grouped launch (autotuned, CUDA graph) against the same
+    problems launched one by one."""
+    import torch
+
+    import beamforming_gb300 as bf
+
+    torch.cuda.set_device(0)
+    shapes = batched_problems()
+    probs = []
+    total_cmac = 0
+    for i, (T, F, D, B) in enumerate(shapes):
+        d = bf.Dims(T, F, D, 2, B)
+        E = torch.empty(d.esize, dtype=torch.uint8, device="cuda")
+        A = torch.empty(d.asize, dtype=torch.uint8, device="cuda")
+        bf.fill_random_device(E, 2, 2 + 2 * i)  # seed 2; streams 2i+2 (E) and 2i+3 (A)
+        bf.fill_random_device(A, 2, 3 + 2 * i)
+        G = torch.from_numpy(bf.gains(d)).cuda()
+        W = bf.ResidentWeights(F, B, D, A, G)
+        J = torch.empty(d.jsize, dtype=torch.uint8, device="cuda")
+        probs.append((d, W, E, J))
+        total_cmac += d.cmacs
+    stream = torch.cuda.current_stream()
+
+    def per_problem():
+        for d, W, E, J in probs:
+            W.form_beams(J, E, d.ntimes, stream=stream)
+
+    per_problem()
+    bf.stream_status(stream)
+    ref = [bf.adler32_device(J) for _, _, _, J in probs]
+    batch = bf.Batch([(W, d.ntimes, E, J) for d, W, E, J in probs], stream=stream)
+    batch.run(stream)
+    bf.stream_status(stream)
+    assert [bf.adler32_device(J) for _, _, _, J in probs] == ref, "batched launch differs from per-problem launches"
+
+    def timed(fn):
+        for _ in range(max(3, args.warmup)):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        bf.stream_status(stream)
+        return e0.elapsed_time(e1) / args.steps
+
+    ms_batch = timed(lambda: batch.run(stream))
+    ms_loop = timed(per_problem)
+    alg_bytes = sum(d.esize + d.jsize + d.asize + 4 * d.gsize for d, _, _, _ in probs)
+    peak, peak_kind = load_peaks()
+    line = {
+        "metric": METRIC,
+        "value": total_cmac / (ms_batch * 1e-3),
+        "unit": UNIT,
+        "n_gpus": 1,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms_batch, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "int4 complex in, exact integer sums (e4m3 tensor-core operands, f32 accumulate)",
+        "data": "synthetic (seeded uniform 4-bit complex; G from the reference setup() formula)",
+        "config": {"workload": BATCH_NAME, "problems": len(probs), "total_cmac": total_cmac},
+        "per_problem_launches": {"value": total_cmac / (ms_loop * 1e-3), "ms_per_step": round(ms_loop, 4),
+                                 "launches": len(probs)},
+        "speedup_vs_per_problem": round(ms_loop / ms_batch, 3),
+        "roofline": {"bound": "hbm", "achieved": round(alg_bytes / (ms_batch * 1e-3) / 1e9, 1), "peak": peak,
+                     "peak_kind": f"{peak_kind} (copy bandwidth)", "unit": "GB/s",
+                     "frac": round(alg_bytes / (ms_batch * 1e-3) / 1e9 / peak, 4)},
+        "autotune": batch.info(),
+        "parity": "per-problem adler32 of the batched launch equals the per-problem launches",
+        "gpu_launches": args.steps,
+    }
+    print(json.dumps(line), flush=True)
+    batch.close()
+
+
 def main():
     args = parse_args()
+    if args.workload == "batched":
+        run_batched(args)
+        return
     if args.frequencies:
         WORKLOAD["nfrequencies"] = args.frequencies
         global WORKLOAD_NAME
