@@ -58,6 +58,12 @@ EXPORTED_SYMBOLS = (
     "bf_batch_run",
     "bf_batch_info",
     "bf_batch_destroy",
+    "bf_server_create",
+    "bf_server_submit",
+    "bf_server_wait",
+    "bf_server_drain",
+    "bf_server_stats_get",
+    "bf_server_destroy",
     "bf_adler32_device",
     "bf_fill_random_device",
     "bf_fill_random_host",
@@ -162,6 +168,13 @@ def lib() -> ctypes.CDLL:
         L.bf_batch_run.argtypes = [vp, vp]
         L.bf_batch_info.argtypes = [vp] + [ctypes.POINTER(ctypes.c_int)] * 4 + [ctypes.POINTER(ctypes.c_float)]
         L.bf_batch_destroy.argtypes = [vp]
+        L.bf_server_create.argtypes = [ctypes.POINTER(vp), vp, ctypes.POINTER(_ServerConfig)]
+        L.bf_server_submit.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int64, u8p, ctypes.c_int, u8p,
+                                       ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]
+        L.bf_server_wait.argtypes = [vp, ctypes.c_int64, ctypes.POINTER(ctypes.c_double)]
+        L.bf_server_drain.argtypes = [vp]
+        L.bf_server_stats_get.argtypes = [vp, ctypes.POINTER(_ServerStats)]
+        L.bf_server_destroy.argtypes = [vp]
         L.bf_adler32_device.argtypes = [u8p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_uint32), vp]
         L.bf_fill_random_device.argtypes = [u8p, ctypes.c_size_t, ctypes.c_uint64, ctypes.c_uint64, vp]
         L.bf_fill_random_host.argtypes = [u8p, ctypes.c_size_t, ctypes.c_uint64, ctypes.c_uint64]
@@ -318,6 +331,71 @@ class ResidentWeights:
     def close(self) -> None:
         if getattr(self, "_h", None):
             lib().bf_weights_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class _ServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_int64), ("max_batch", ctypes.c_int), ("max_inflight", ctypes.c_int),
+                ("spin_wait", ctypes.c_int)]
+
+
+class _ServerStats(ctypes.Structure):
+    _fields_ = [
+        (n, ctypes.c_int64)
+        for n in ("submitted", "completed", "batches", "chunks_launched", "max_batch_seen", "pool_bytes",
+                  "pool_peak_bytes")
+    ]
+
+
+class Server:
+    """Continuous-batching server over resident weights: ``submit`` chunks as
+    they arrive, ``wait`` for a ticket (latency in seconds), ``drain``.  The
+    server reads E and writes J after ``submit`` returns; the wrapper keeps
+    the buffers referenced until the ticket is waited for (host buffers
+    should be pinned for the copies to overlap)."""
+
+    def __init__(self, weights: "ResidentWeights", hbm_budget_bytes: int = 0, max_batch: int = 0,
+                 max_inflight: int = 0, spin_wait: bool = False):
+        self.weights = weights
+        cfg = _ServerConfig(hbm_budget_bytes, max_batch, max_inflight, int(spin_wait))
+        h = ctypes.c_void_p()
+        _check(lib().bf_server_create(ctypes.byref(h), weights._h, ctypes.byref(cfg)), "bf_server_create")
+        self._h = h
+        self._live: dict[int, tuple] = {}
+
+    def submit(self, channel: int, ntimes: int, E, J, nchannels: int = 1) -> int:
+        w = self.weights
+        pe, ke = _ptr(E, np.uint8, ntimes * nchannels * w.ndishes * 2)
+        pj, kj = _ptr(J, np.uint8, w.nbeams * nchannels * 2 * ntimes, writable=True)
+        t = ctypes.c_int64()
+        _check(lib().bf_server_submit(self._h, channel, nchannels, ntimes, pe, ke, pj, kj, ctypes.byref(t)),
+               "bf_server_submit")
+        self._live[t.value] = (E, J)
+        return t.value
+
+    def wait(self, ticket: int) -> float:
+        lat = ctypes.c_double()
+        _check(lib().bf_server_wait(self._h, ticket, ctypes.byref(lat)), "bf_server_wait")
+        self._live.pop(ticket, None)
+        return lat.value
+
+    def drain(self) -> None:
+        _check(lib().bf_server_drain(self._h), "bf_server_drain")
+
+    def stats(self) -> dict:
+        st = _ServerStats()
+        _check(lib().bf_server_stats_get(self._h, ctypes.byref(st)), "bf_server_stats_get")
+        return {n: getattr(st, n) for n, _ in _ServerStats._fields_}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().bf_server_destroy(self._h)
             self._h = None
 
     def __del__(self):

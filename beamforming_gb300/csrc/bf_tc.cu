@@ -40,6 +40,7 @@
 #include "bf_ptx.cuh"
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <cudaTypedefs.h>
@@ -564,15 +565,16 @@ __global__ void bf_prep_weights(const uint8_t *__restrict__ A, uint8_t *__restri
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 get_encode_fn() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  if (!fn) {
+  // initialised once, thread-safely (the server thread encodes maps too)
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = []() -> PFN_cuTensorMapEncodeTiled_v12000 {
     void *ptr = nullptr;
     cudaDriverEntryPointQueryResult q{};
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
             cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(ptr);
-  }
+      return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(ptr);
+    return nullptr;
+  }();
   return fn;
 }
 
@@ -592,13 +594,12 @@ int g_plan_wslots = 0;  // nonzero: W slots to use (tuning)
 int g_plan_raw = 0;     // nonzero: raw E slots to use (tuning)
 
 int num_sms() {
-  static int n = 0;
-  if (n == 0) {
-    int dev = 0;
+  static const int n = []() {
+    int dev = 0, k = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (n <= 0) n = 1;
-  }
+    cudaDeviceGetAttribute(&k, cudaDevAttrMultiProcessorCount, dev);
+    return k > 0 ? k : 1;
+  }();
   return n;
 }
 
@@ -675,18 +676,19 @@ static cudaError_t make_problem(TcProblem &P, const TcWeights &w, int64_t T, uin
 }
 
 // Ring depths and shared memory for a launch whose largest pass has max_nb_pass beams.
-static cudaError_t plan_launch(TcParams &p, int max_nb_pass, int *smem_bytes) {
+static cudaError_t plan_launch(TcParams &p, int max_nb_pass, const TcRingPlan &plan, int *smem_bytes) {
   // unpacked stages live in the TMEM columns beside the two accumulators; raw E
   // slots take the shared memory the W slots leave
   const int per_half = (kAccCols - 2 * max_nb_pass) / kStageCols;
   const int stages = std::min(kMaxStages, 2 * per_half);
   if (stages < 2) return cudaErrorInvalidValue;
   // shared memory: W slots first (their loads gate the MMA), then raw E slots
-  int wslots = g_plan_wslots > 0 ? g_plan_wslots : kMaxWSlots;
-  int raw = g_plan_raw > 0 ? g_plan_raw : kMinRaw;
+  const int want_w = plan.wslots > 0 ? plan.wslots : g_plan_wslots;
+  const int want_r = plan.raw > 0 ? plan.raw : g_plan_raw;
+  int wslots = want_w > 0 ? want_w : kMaxWSlots;
+  int raw = want_r > 0 ? want_r : kMinRaw;
   while (wslots > 2 && smem_plan(stages, wslots, raw, max_nb_pass).total + 1024 > kSmemLimit) --wslots;
-  while (raw < kMaxRaw && smem_plan(stages, wslots, raw + 1, max_nb_pass).total + 1024 <= kSmemLimit &&
-         g_plan_raw <= 0)
+  while (raw < kMaxRaw && smem_plan(stages, wslots, raw + 1, max_nb_pass).total + 1024 <= kSmemLimit && want_r <= 0)
     ++raw;
   while (raw > 2 && smem_plan(stages, wslots, raw, max_nb_pass).total + 1024 > kSmemLimit) --raw;
   p.max_nb_pass = max_nb_pass;
@@ -700,12 +702,12 @@ static cudaError_t plan_launch(TcParams &p, int max_nb_pass, int *smem_bytes) {
 
 template <bool kGrouped>
 static cudaError_t launch_kernel(const TcParams &p, int smem_bytes, cudaStream_t s) {
-  static bool attr_set = false;
-  if (!attr_set) {
+  static std::atomic<bool> attr_set{false};
+  if (!attr_set.load()) {
     const cudaError_t e =
         cudaFuncSetAttribute(bf_form_beams_tc<kGrouped>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
     if (e != cudaSuccess) return e;
-    attr_set = true;
+    attr_set.store(true);
   }
   const int grid = std::min(p.ntiles, num_sms());
   if (grid <= 0) return cudaSuccess;
@@ -730,13 +732,8 @@ cudaError_t launch_tc_grouped(const TcProblem *table, int nprob, int ntiles, int
   p.ntiles = ntiles;
   p.nk = tc_stages_per_tile(D);
   p.err = err;
-  const int save_w = g_plan_wslots, save_r = g_plan_raw;
-  if (plan.wslots > 0) g_plan_wslots = plan.wslots;
-  if (plan.raw > 0) g_plan_raw = plan.raw;
   int smem_bytes = 0;
-  const cudaError_t e = plan_launch(p, max_nb_pass, &smem_bytes);
-  g_plan_wslots = save_w;
-  g_plan_raw = save_r;
+  const cudaError_t e = plan_launch(p, max_nb_pass, plan, &smem_bytes);
   if (e != cudaSuccess) return e;
   return launch_kernel<true>(p, smem_bytes, s);
 }
@@ -753,7 +750,7 @@ cudaError_t launch_tc(const TcWeights &w, int64_t T, uint8_t *J, const uint8_t *
   p.nk = tc_stages_per_tile(w.D);
   p.err = err;
   int smem_bytes = 0;
-  e = plan_launch(p, w.nb_pass, &smem_bytes);
+  e = plan_launch(p, w.nb_pass, TcRingPlan{}, &smem_bytes);
   if (e != cudaSuccess) return e;
   return launch_kernel<false>(p, smem_bytes, s);
 }

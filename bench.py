@@ -55,10 +55,24 @@ def parse_args():
     ap.add_argument("--frequencies", type=int, default=None, help="override f (profiling a smaller case)")
     ap.add_argument(
         "--workload",
-        choices=["chunk", "batched"],
+        choices=["chunk", "batched", "served"],
         default="chunk",
-        help="chunk: the full single-GPU chunk (default); batched: 128 uneven problems in one persistent launch",
+        help="chunk: the full single-GPU chunk (default); batched: 128 uneven problems in one persistent launch; "
+        "served: the Poisson chunk stream through the continuous-batching server against the plain loop",
     )
+    ap.add_argument("--rate", type=float, default=None, help="served: arrival rate (chunks/s)")
+    ap.add_argument("--duration", type=float, default=None, help="served: stream length (s)")
+    ap.add_argument("--contents", type=int, default=128, help="served: distinct chunks the stream draws from")
+    ap.add_argument("--slots", type=int, default=512, help="served: pinned J slots in the ring")
+    ap.add_argument("--check-threads", type=int, default=6, help="served: threads checking landed chunks")
+    ap.add_argument("--saturation-chunks", type=int, default=4000, help="served: chunks in the back-to-back run")
+    ap.add_argument("--extra-rates", type=float, nargs="*", default=[8000.0],
+                    help="served: further Poisson rates (chunks/s) run for --extra-duration seconds each")
+    ap.add_argument("--extra-duration", type=float, default=5.0)
+    ap.add_argument("--no-spin", action="store_true",
+                    help="served: server threads sleep between launches instead of polling (both loops)")
+    ap.add_argument("--max-batch", type=int, default=64, help="served: chunks per grouped launch")
+    ap.add_argument("--max-inflight", type=int, default=3, help="served: launches in flight")
     return ap.parse_args()
 
 
@@ -520,10 +534,233 @@ def run_batched(args):
     batch.close()
 
 
+SERVED = {"channels": 64, "nbeams": 96, "ndishes": 512, "npolarizations": 2, "rate_hz": 2000.0, "duration_s": 30.0,
+          "ntimes": [1024, 2048, 4096, 8192, 16384], "seed": 3}
+SERVED_NAME = ("served stream: Poisson arrivals at 2000 chunks/s for 30 s over f=64 channels (b=96 d=512 p=2, "
+               "weights resident), one channel per chunk, t uniform over {1024..16384}, seed 3")
+
+
+def served_setup(bf, torch, ncontents):
+    """Resident weights for all channels, and `ncontents` distinct chunks (a
+    channel, t and E each, drawn from seed 3) in pinned host memory.  Each
+    chunk's expected adler32 comes from its own plain launch: a per-channel
+    resident-weights pass on the device."""
+    S = SERVED
+    F, B, D = S["channels"], S["nbeams"], S["ndishes"]
+    dall = bf.Dims(16, F, D, 2, B)
+    A = torch.empty(dall.asize, dtype=torch.uint8, device="cuda")
+    bf.fill_random_device(A, S["seed"], 1)
+    G = torch.from_numpy(bf.gains(dall)).cuda()
+    W = bf.ResidentWeights(F, B, D, A, G)
+    rng = np.random.default_rng(S["seed"])
+    per_channel = {}
+    contents = []
+    for k in range(ncontents):
+        c = int(rng.integers(F))
+        T = int(rng.choice(S["ntimes"]))
+        if c not in per_channel:
+            per_channel[c] = bf.ResidentWeights(1, B, D, A[c * B * D:(c + 1) * B * D], G[c * B:(c + 1) * B])
+        Ed = torch.empty(T * D * 2, dtype=torch.uint8, device="cuda")
+        bf.fill_random_device(Ed, S["seed"], 2 + k)
+        Jd = torch.empty(B * 2 * T, dtype=torch.uint8, device="cuda")
+        per_channel[c].form_beams(Jd, Ed, T)
+        bf.stream_status()
+        Eh = torch.empty(T * D * 2, dtype=torch.uint8, pin_memory=True)
+        Eh.copy_(Ed)
+        contents.append((c, T, Eh.numpy(), bf.adler32_device(Jd)))
+    for w in per_channel.values():
+        w.close()
+    torch.cuda.synchronize()
+    return W, contents
+
+
+def serve_stream(bf, torch, W, contents, arrivals, picks, cfg, nslots, check_threads):
+    """Submits chunk `picks[i]` at time `arrivals[i]` (seconds from the start;
+    all zero: back to back) to a server with config `cfg`, checks every
+    landed J against its expected adler32, and returns the measurements."""
+    import queue
+    import threading
+    import zlib
+    from concurrent.futures import ThreadPoolExecutor
+
+    B = SERVED["nbeams"]
+    n = len(arrivals)
+    jbytes = np.array([B * 2 * contents[k][1] for k in picks], dtype=np.int64)
+    if nslots >= n:
+        # one packed J region per chunk, checked after the stream (no slot ever waits)
+        offs = np.concatenate([[0], np.cumsum(jbytes)])
+        nslots = n
+    else:
+        # a ring of equal slots, each checked and freed as its chunk lands
+        maxj = B * 2 * max(T for _, T, _, _ in contents)
+        offs = np.arange(nslots + 1, dtype=np.int64) * maxj
+    ring = torch.empty(int(offs[-1]), dtype=torch.uint8, pin_memory=True).numpy()
+    deferred = nslots == n
+    free = [threading.Event() for _ in range(nslots)]
+    for e in free:
+        e.set()
+    lat = np.zeros(n)
+    late = np.zeros(n)
+    bad = []
+    srv = bf.Server(W, **cfg)
+    handoff: queue.Queue = queue.Queue()
+    pool = ThreadPoolExecutor(check_threads)
+    stalls = 0
+
+    def check(i, slot, jb, want):
+        if zlib.adler32(ring[offs[slot]:offs[slot] + jb]) != want:
+            bad.append(i)
+        free[slot].set()
+
+    def collector():
+        for _ in range(n):
+            i, t, slot, jb, want = handoff.get()
+            lat[i] = srv.wait(t)
+            if not deferred:
+                pool.submit(check, i, slot, jb, want)
+
+    # the submitter spins on the clock holding the GIL; hand the GIL to the
+    # collector and checker threads quickly
+    switch = sys.getswitchinterval()
+    sys.setswitchinterval(5e-5)
+    th = threading.Thread(target=collector)
+    th.start()
+    t0 = time.perf_counter()
+    for i in range(n):
+        c, T, Eh, want = contents[picks[i]]
+        slot = i % nslots
+        if not free[slot].is_set():
+            stalls += 1
+            free[slot].wait()
+        free[slot].clear()
+        due = t0 + arrivals[i]
+        now = time.perf_counter()
+        if due - now > 3e-4:
+            time.sleep(due - now - 2e-4)
+        while time.perf_counter() < due:
+            pass
+        jb = int(jbytes[i])
+        tk = srv.submit(c, T, Eh, ring[offs[slot]:offs[slot] + jb])
+        late[i] = time.perf_counter() - due
+        handoff.put((i, tk, slot, jb, want))
+    srv.drain()
+    t1 = time.perf_counter()
+    th.join()
+    if deferred:
+        for i in range(n):
+            pool.submit(check, i, i, int(jbytes[i]), contents[picks[i]][3])
+    pool.shutdown(wait=True)
+    sys.setswitchinterval(switch)
+    st = srv.stats()
+    srv.close()
+    Ts = np.array([contents[k][1] for k in picks])
+    beam_samples = int(B * 2 * Ts.sum())
+    cmac = int(B * 2 * SERVED["ndishes"] * Ts.sum())
+    pct = lambda a, q: round(float(np.percentile(a, q)) * 1e3, 3)  # noqa: E731
+    return {
+        "chunks": n,
+        "wall_s": round(t1 - t0, 3),
+        "chunks_per_s": round(n / (t1 - t0), 1),
+        "beam_samples_per_s": beam_samples / (t1 - t0),
+        "cmac_per_s": cmac / (t1 - t0),
+        "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99), "p99.9": pct(lat, 99.9), "max": pct(lat, 100),
+                       "mean": round(float(lat.mean()) * 1e3, 3)},
+        "submit_lateness_ms": {"p50": pct(late, 50), "p99": pct(late, 99)},
+        "slot_stalls": stalls,
+        "mismatches": len(bad),
+        "server": {k: st[k] for k in ("batches", "max_batch_seen", "pool_bytes", "pool_peak_bytes")},
+        "config": {k: v for k, v in cfg.items()},
+    }
+
+
+def run_served(args):
+    """The served stream against the plain per-chunk loop (the same server
+    thread with one chunk per launch and one launch in flight), at the
+    stream's Poisson rate, then back to back (saturation)."""
+    import torch
+
+    import beamforming_gb300 as bf
+
+    torch.cuda.set_device(0)
+    S = SERVED
+    rate = args.rate or S["rate_hz"]
+    duration = args.duration or S["duration_s"]
+    W, contents = served_setup(bf, torch, args.contents)
+    rng = np.random.default_rng(S["seed"] + 1000)
+    n = int(round(rate * duration))
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
+    arrivals -= arrivals[0]
+    picks = rng.integers(len(contents), size=n)
+    nsat = args.saturation_chunks
+    sat_picks = rng.integers(len(contents), size=nsat)
+    served_cfg = {"max_batch": args.max_batch, "max_inflight": args.max_inflight, "spin_wait": not args.no_spin}
+    plain_cfg = {"max_batch": 1, "max_inflight": 1, "spin_wait": not args.no_spin}
+    out = {}
+    try:
+        gpu_id = "GPU-" + str(torch.cuda.get_device_properties(0).uuid)
+    except Exception:
+        gpu_id = None
+    clocks = ClockSampler(gpu_id)
+    clocks.start()
+    for name, cfg in (("served", served_cfg), ("plain", plain_cfg)):
+        serve_stream(bf, torch, W, contents, np.zeros(min(200, n)), picks[:200], cfg, args.slots,
+                     args.check_threads)  # warm-up
+        out[name] = serve_stream(bf, torch, W, contents, arrivals, picks, cfg, args.slots, args.check_threads)
+        out[name + "_saturation"] = serve_stream(bf, torch, W, contents, np.zeros(nsat), sat_picks, cfg, nsat,
+                                                 args.check_threads)
+        del out[name + "_saturation"]["submit_lateness_ms"]  # every chunk is due at once
+    for rate_x in args.extra_rates:
+        nx = int(round(rate_x * args.extra_duration))
+        arr_x = np.cumsum(rng.exponential(1.0 / rate_x, nx))
+        arr_x -= arr_x[0]
+        picks_x = rng.integers(len(contents), size=nx)
+        for name, cfg in (("served", served_cfg), ("plain", plain_cfg)):
+            r = serve_stream(bf, torch, W, contents, arr_x, picks_x, cfg, args.slots, args.check_threads)
+            out.setdefault("load_sweep", []).append({"rate_hz": rate_x, "loop": name, **{
+                k: r[k] for k in ("chunks", "chunks_per_s", "beam_samples_per_s", "latency_ms", "submit_lateness_ms",
+                                  "mismatches")}})
+    clk = clocks.stop()
+    sv, pl = out["served"], out["plain"]
+    line = {
+        "metric": "beam samples/s and p50/p99/p99.9 chunk latency (served stream)",
+        "value": sv["beam_samples_per_s"],
+        "unit": "beam samples/s",
+        "n_gpus": 1,
+        "steps": n,
+        "warmup": 200,
+        "ms_per_step": round(sv["wall_s"] * 1e3 / n, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "int4 complex in, exact integer sums (e4m3 tensor-core operands, f32 accumulate)",
+        "data": "synthetic (seeded uniform 4-bit complex; G from the reference setup() formula)",
+        "config": {"workload": SERVED_NAME, "rate_hz": rate, "duration_s": duration,
+                   "distinct_chunks": len(contents), "buffers": "E and J in pinned host memory, copies inside"},
+        "served": sv,
+        "plain_loop": pl,
+        "served_saturation": out["served_saturation"],
+        "plain_saturation": out["plain_saturation"],
+        "load_sweep": out.get("load_sweep", []),
+        "p99_ratio_plain_over_served": round(pl["latency_ms"]["p99"] / sv["latency_ms"]["p99"], 3),
+        "saturation_speedup": round(out["served_saturation"]["beam_samples_per_s"]
+                                    / out["plain_saturation"]["beam_samples_per_s"], 3),
+        "parity": "every landed chunk's adler32 equals its plain per-chunk launch's",
+        "mismatches": sum(x["mismatches"] for x in (sv, pl, out["served_saturation"], out["plain_saturation"]))
+        + sum(x["mismatches"] for x in out.get("load_sweep", [])),
+        "clocks": clk,
+        "gpu_launches": sv["server"]["batches"],
+    }
+    print(json.dumps(line), flush=True)
+    W.close()
+
+
 def main():
     args = parse_args()
     if args.workload == "batched":
         run_batched(args)
+        return
+    if args.workload == "served":
+        run_served(args)
         return
     if args.frequencies:
         WORKLOAD["nfrequencies"] = args.frequencies

@@ -171,6 +171,52 @@ BF_API int bf_batch_info(const bf_batch *batch, int *ntiles, int *order, int *ws
 
 BF_API int bf_batch_destroy(bf_batch *batch);
 
+/* ---------------------------------------------------------------- serving */
+
+/* A served stream of voltage chunks with continuous batching.  No
+ * counterpart in the reference.  A server thread admits submitted chunks while
+ * a fixed HBM pool has room for their buffers, packs them into one grouped
+ * tensor-core launch, and keeps up to max_inflight launches in flight, so
+ * chunks that arrive while others run are admitted as memory and launch slots
+ * free up.  The resident weights must not be updated while chunks are in
+ * flight (drain first). */
+typedef struct bf_server bf_server;
+
+typedef struct bf_server_config {
+  int64_t hbm_budget_bytes; /* device pool for chunk buffers; 0: half of the free HBM */
+  int max_batch;            /* chunks per grouped launch; 0: 64 (1: plain per-chunk launches) */
+  int max_inflight;         /* launches in flight; 0: 3 */
+  int spin_wait;            /* 1: the server thread polls launches instead of sleeping until a host
+                               callback wakes it (lower latency; keeps one host core busy) */
+} bf_server_config;
+
+typedef struct bf_server_stats {
+  int64_t submitted, completed;
+  int64_t batches, chunks_launched, max_batch_seen;
+  int64_t pool_bytes, pool_peak_bytes;
+} bf_server_stats;
+
+/* Creates a server over resident weights (all channels = the weights' frequencies). */
+BF_API int bf_server_create(bf_server **out, const bf_weights *weights, const bf_server_config *config);
+
+/* Submits one chunk: channels [channel, channel + nchannels) of ntimes samples,
+ * E[t][c][d][p] and J[b][c][p][t] in host memory (pinned for overlap) or device
+ * memory (e_on_device / j_on_device).  Returns at once with a ticket; the
+ * arrival time is now.  Needs ntimes % 16 == 0. */
+BF_API int bf_server_submit(bf_server *server, int channel, int nchannels, int64_t ntimes, const uint8_t *E,
+                            int e_on_device, uint8_t *J, int j_on_device, int64_t *ticket);
+
+/* Blocks until the ticket's chunk is complete (J written); returns its latency
+ * (submission to completion) in seconds. */
+BF_API int bf_server_wait(bf_server *server, int64_t ticket, double *latency_s);
+
+/* Blocks until every submitted chunk is complete. */
+BF_API int bf_server_drain(bf_server *server);
+
+BF_API int bf_server_stats_get(bf_server *server, bf_server_stats *stats);
+
+BF_API int bf_server_destroy(bf_server *server);
+
 /* ------------------------------------------------------- no allocation */
 
 /* No counterpart in the reference.  For callers that cannot allocate device

@@ -66,6 +66,14 @@ def test_invalid_arguments(bflib):
     assert L.bf_form_beams_ex(ctypes.byref(d0), None, None, None, None, 0, None) == bflib.OK
     out = ctypes.c_uint32()
     assert L.bf_adler32_device(None, 0, ctypes.byref(out), None) == bflib.OK and out.value == 1
+    # server entry points check their handles before touching a device
+    h = ctypes.c_void_p()
+    assert L.bf_server_create(ctypes.byref(h), None, None) == bflib.ERR_INVALID_ARGUMENT
+    t = ctypes.c_int64()
+    assert L.bf_server_submit(None, 0, 1, 16, None, 0, None, 0, ctypes.byref(t)) == bflib.ERR_INVALID_ARGUMENT
+    assert L.bf_server_wait(None, 0, None) == bflib.ERR_INVALID_ARGUMENT
+    assert L.bf_server_drain(None) == bflib.ERR_INVALID_ARGUMENT
+    assert L.bf_server_destroy(None) == bflib.OK
 
 
 def test_python_argument_checks(bflib):
