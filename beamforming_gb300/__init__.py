@@ -58,8 +58,10 @@ EXPORTED_SYMBOLS = (
     "bf_batch_run",
     "bf_batch_info",
     "bf_batch_destroy",
+    "bf_tensor_peak",
     "bf_server_create",
     "bf_server_submit",
+    "bf_server_update_weights",
     "bf_server_wait",
     "bf_server_drain",
     "bf_server_stats_get",
@@ -171,6 +173,8 @@ def lib() -> ctypes.CDLL:
         L.bf_server_create.argtypes = [ctypes.POINTER(vp), vp, ctypes.POINTER(_ServerConfig)]
         L.bf_server_submit.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int64, u8p, ctypes.c_int, u8p,
                                        ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]
+        L.bf_tensor_peak.argtypes = [ctypes.POINTER(ctypes.c_double), vp]
+        L.bf_server_update_weights.argtypes = [vp, u8p, fp, ctypes.c_int]
         L.bf_server_wait.argtypes = [vp, ctypes.c_int64, ctypes.POINTER(ctypes.c_double)]
         L.bf_server_drain.argtypes = [vp]
         L.bf_server_stats_get.argtypes = [vp, ctypes.POINTER(_ServerStats)]
@@ -349,7 +353,7 @@ class _ServerStats(ctypes.Structure):
     _fields_ = [
         (n, ctypes.c_int64)
         for n in ("submitted", "completed", "batches", "chunks_launched", "max_batch_seen", "pool_bytes",
-                  "pool_peak_bytes")
+                  "pool_peak_bytes", "weight_updates")
     ]
 
 
@@ -378,6 +382,15 @@ class Server:
                "bf_server_submit")
         self._live[t.value] = (E, J)
         return t.value
+
+    def update_weights(self, A, G) -> None:
+        """New weights for chunks submitted from now on (no drain)."""
+        w = self.weights
+        pa, ka = _ptr(A, np.uint8, w.nfrequencies * w.nbeams * w.ndishes)
+        pg, kg = _ptr(G, np.float32, 4 * w.nfrequencies * w.nbeams)
+        if ka != kg:
+            raise ValueError("A and G must both be host arrays or both CUDA tensors")
+        _check(lib().bf_server_update_weights(self._h, pa, pg, ka), "bf_server_update_weights")
 
     def wait(self, ticket: int) -> float:
         lat = ctypes.c_double()
@@ -459,6 +472,13 @@ class Batch:
 
 
 # ---------------------------------------------------------------- checksum
+
+
+def tensor_peak_tflops(stream=None) -> float:
+    """Measured dense E4M3 tcgen05 MMA rate of the current device (TFLOP/s)."""
+    out = ctypes.c_double()
+    _check(lib().bf_tensor_peak(ctypes.byref(out), _stream_handle(stream)), "bf_tensor_peak")
+    return out.value
 
 
 def adler32_device(data, nbytes: int | None = None, stream=None) -> int:

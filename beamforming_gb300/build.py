@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libbeamform.so")
-SOURCES = ["bf_api.cu", "bf_simt.cu", "bf_tc.cu", "bf_adler.cu", "bf_noalloc.cu", "bf_batch.cu", "bf_server.cu"]
+SOURCES = ["bf_api.cu", "bf_simt.cu", "bf_tc.cu", "bf_adler.cu", "bf_noalloc.cu", "bf_batch.cu", "bf_server.cu", "bf_peak.cu"]
 HEADERS = ["bf_internal.h", "bf_ptx.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [

@@ -86,6 +86,7 @@ class Pool {
 
 struct Request {
   int64_t ticket;
+  int version;  // weight version the chunk was submitted under
   int channel, nchannels;
   int64_t ntimes;
   const uint8_t *E;
@@ -112,6 +113,17 @@ struct Flight {
   Clock::time_point landed_at;
 };
 
+// A weight version: version 0 is the caller's resident weights (never
+// written); later versions are server-owned copies refreshed in turn.  A
+// version is rewritten only when no queued or in-flight chunk refers to it.
+constexpr int kMaxVersions = 4;
+struct Version {
+  const bf_weights *w = nullptr;
+  bf_weights *owned = nullptr;
+  int64_t refs = 0;              // chunks submitted under this version and not yet landed
+  cudaEvent_t ready = nullptr;   // recorded behind the refresh on the update stream
+};
+
 }  // namespace
 
 struct bf_server {
@@ -120,6 +132,10 @@ struct bf_server {
   bf_server_config cfg{};
   Pool pool;
   std::vector<std::unique_ptr<Flight>> flights;
+  Version ver[kMaxVersions];
+  int cur = 0;                      // version new chunks are submitted under
+  cudaStream_t upd_stream = nullptr;
+  std::mutex upd_mu;                // one refresh at a time
 
   std::mutex mu;  // guards everything below, the pool and the flights' busy/landed/reqs
   std::condition_variable cv_work, cv_done;
@@ -171,11 +187,17 @@ void CUDART_CB flight_landed(void *arg) {
 bool bf_server::launch(Flight &fl, const std::vector<Request> &reqs, int *ntiles) {
   const TcWeights &w = weights->tc;
   int64_t begin = 0;
+  unsigned waited = 0;  // versions whose refresh this stream already waits for
   for (size_t i = 0; i < reqs.size(); ++i) {
     const Request &r = reqs[i];
+    const Version &vr = ver[r.version];  // stable: the chunk holds a reference
+    if (vr.ready && !(waited & (1u << r.version))) {
+      if (cudaStreamWaitEvent(fl.s, vr.ready, 0) != cudaSuccess) return false;
+      waited |= 1u << r.version;
+    }
     if (!r.e_on_device && cudaMemcpyAsync(r.dE, r.E, r.e_bytes, cudaMemcpyHostToDevice, fl.s) != cudaSuccess)
       return false;
-    const TcWeights v = channel_view(w, r.channel, r.nchannels);
+    const TcWeights v = channel_view(vr.w->tc, r.channel, r.nchannels);
     TcProblem &P = fl.table_host[i];
     if (tc_make_problem(P, v, r.ntimes, r.dJ, r.e_on_device ? r.E : r.dE, 0) != cudaSuccess) return false;
     P.tile_begin = static_cast<int>(begin);
@@ -204,6 +226,7 @@ bool bf_server::launch(Flight &fl, const std::vector<Request> &reqs, int *ntiles
 void bf_server::finish_locked(Flight &fl) {
   if (*fl.err_host != 0 && status == BF_OK) status = BF_ERR_DEVICE_TIMEOUT;  // a kernel wait gave up
   for (Request &r : fl.reqs) {
+    --ver[r.version].refs;
     if (!r.e_on_device) pool.release(r.dE, r.e_bytes);
     if (!r.j_on_device) pool.release(r.dJ, r.j_bytes);
     done_latency[r.ticket] = std::chrono::duration<double>(fl.landed_at - r.arrival).count();
@@ -320,6 +343,7 @@ int bf_server_create(bf_server **out, const bf_weights *weights, const bf_server
   bf_server *s = new bf_server();
   cudaGetDevice(&s->device);
   s->weights = weights;
+  s->ver[0].w = weights;
   if (cfg) s->cfg = *cfg;
   if (s->cfg.max_batch <= 0) s->cfg.max_batch = 64;
   if (s->cfg.max_inflight <= 0) s->cfg.max_inflight = 3;
@@ -329,6 +353,8 @@ int bf_server_create(bf_server **out, const bf_weights *weights, const bf_server
   budget = std::min(budget, free_b * 9 / 10);
   s->cfg.hbm_budget_bytes = static_cast<int64_t>(budget);
   if (st == BF_OK && !s->pool.init(budget)) st = BF_ERR_OUT_OF_MEMORY;
+  if (st == BF_OK && cudaStreamCreateWithFlags(&s->upd_stream, cudaStreamNonBlocking) != cudaSuccess)
+    st = BF_ERR_CUDA;
   for (int i = 0; st == BF_OK && i < s->cfg.max_inflight; ++i) {
     s->flights.push_back(std::make_unique<Flight>());
     Flight &fl = *s->flights.back();
@@ -379,12 +405,49 @@ int bf_server_submit(bf_server *s, int channel, int nchannels, int64_t ntimes, c
     std::lock_guard<std::mutex> lk(s->mu);
     if (s->status != BF_OK) return s->status;
     r.ticket = s->next_ticket++;
+    r.version = s->cur;
+    ++s->ver[s->cur].refs;
     ++s->submitted;
     s->queue.push_back(r);
     s->nqueued.fetch_add(1, std::memory_order_release);
   }
   s->cv_work.notify_one();
   *ticket = r.ticket;
+  return BF_OK;
+}
+
+int bf_server_update_weights(bf_server *s, const uint8_t *A, const float *G, int ptr_kind) {
+  if (!s || !A || !G || (ptr_kind != BF_PTR_HOST && ptr_kind != BF_PTR_DEVICE)) return BF_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> one(s->upd_mu);
+  // a version slot other than the caller's weights and the current one, with no chunk on it
+  int slot = -1;
+  {
+    std::unique_lock<std::mutex> lk(s->mu);
+    for (;;) {
+      if (s->status != BF_OK) return s->status;
+      for (int i = 1; i < kMaxVersions && slot < 0; ++i)
+        if (i != s->cur && s->ver[i].refs == 0) slot = i;
+      if (slot >= 0) break;
+      s->cv_done.wait_for(lk, std::chrono::milliseconds(50));  // every version busy: wait for chunks to land
+    }
+  }
+  Version &v = s->ver[slot];
+  const TcWeights &w = s->weights->tc;
+  int st = BF_OK;
+  if (!v.owned) {
+    st = bf_weights_create(&v.owned, w.F, w.B, w.D, A, G, ptr_kind, s->upd_stream);
+    if (st == BF_OK && cudaEventCreateWithFlags(&v.ready, cudaEventDisableTiming) != cudaSuccess) st = BF_ERR_CUDA;
+  } else {
+    st = bf_weights_update(v.owned, A, G, ptr_kind, s->upd_stream);
+  }
+  if (st != BF_OK) return st;
+  if (cudaEventRecord(v.ready, s->upd_stream) != cudaSuccess) return BF_ERR_CUDA;
+  // the caller may reuse or free A and G once this returns
+  if (cudaStreamSynchronize(s->upd_stream) != cudaSuccess) return BF_ERR_CUDA;
+  std::lock_guard<std::mutex> lk(s->mu);
+  v.w = v.owned;
+  s->cur = slot;
+  ++s->stats.weight_updates;
   return BF_OK;
 }
 
@@ -441,6 +504,11 @@ int bf_server_destroy(bf_server *s) {
     if (fl.err_dev) cudaFree(fl.err_dev);
     if (fl.err_host) cudaFreeHost(fl.err_host);
   }
+  for (Version &v : s->ver) {
+    if (v.owned) bf_weights_destroy(v.owned);
+    if (v.ready) cudaEventDestroy(v.ready);
+  }
+  if (s->upd_stream) cudaStreamDestroy(s->upd_stream);
   delete s;
   return BF_OK;
 }

@@ -55,11 +55,14 @@ def parse_args():
     ap.add_argument("--frequencies", type=int, default=None, help="override f (profiling a smaller case)")
     ap.add_argument(
         "--workload",
-        choices=["chunk", "batched", "served"],
+        choices=["chunk", "batched", "served", "wide"],
         default="chunk",
         help="chunk: the full single-GPU chunk (default); batched: 128 uneven problems in one persistent launch; "
-        "served: the Poisson chunk stream through the continuous-batching server against the plain loop",
+        "served: the Poisson chunk stream through the continuous-batching server against the plain loop; "
+        "wide: d=1024 b=512 chunks through the server with weight refresh every 8 chunks",
     )
+    ap.add_argument("--chunks", type=int, default=64, help="wide: chunks per round of the timed served loop")
+    ap.add_argument("--rounds", type=int, default=6, help="wide: rounds (J checked between rounds)")
     ap.add_argument("--rate", type=float, default=None, help="served: arrival rate (chunks/s)")
     ap.add_argument("--duration", type=float, default=None, help="served: stream length (s)")
     ap.add_argument("--contents", type=int, default=128, help="served: distinct chunks the stream draws from")
@@ -103,6 +106,13 @@ def profile_traffic():
             except ValueError:
                 return None
     return None
+
+
+def gpu_uuid(torch, index):
+    try:
+        return "GPU-" + str(torch.cuda.get_device_properties(index).uuid)
+    except Exception:
+        return None
 
 
 class ClockSampler:
@@ -252,6 +262,28 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def roofline_of(bf, stream, cmacs, alg_bytes, k_ms, kernel):
+    """Both rooflines of a tensor-core launch: HBM (algorithmic bytes against
+    the measured copy bandwidth) and tensor (8 flops per complex MAC -- the
+    real GEMM embedding does 4 multiply-adds per complex one -- against the
+    dense E4M3 MMA rate measured now).  `bound` is the one with the longer
+    ideal time; `frac` = that ideal time / the measured kernel time."""
+    hbm_peak, hbm_kind = load_peaks()
+    tc_peak = bf.tensor_peak_tflops(stream)
+    k_s = k_ms * 1e-3
+    t_hbm = alg_bytes / (hbm_peak * 1e9)
+    t_tc = 8 * cmacs / (tc_peak * 1e12)
+    hbm = {"achieved": round(alg_bytes / k_s / 1e9, 1), "peak": hbm_peak, "unit": "GB/s",
+           "frac": round(t_hbm / k_s, 4), "peak_kind": f"{hbm_kind} (copy bandwidth)"}
+    tensor = {"achieved": round(8 * cmacs / k_s / 1e12, 1), "peak": round(tc_peak, 1), "unit": "TFLOP/s",
+              "frac": round(t_tc / k_s, 4),
+              "peak_kind": "measured in this run: dense E4M3 tcgen05 MMA stream on every SM (bf_tensor_peak)"}
+    bound = "hbm" if t_hbm >= t_tc else "tensor"
+    main = hbm if bound == "hbm" else tensor
+    return {"bound": bound, "kernel": kernel, **main, "kernel_ms": round(k_ms, 4), "algorithmic_bytes": alg_bytes,
+            "algorithmic_flops": 8 * cmacs, "hbm": hbm, "tensor": tensor}
+
+
 def run_ours(args):
     import torch
 
@@ -287,12 +319,7 @@ def run_ours(args):
     bf.stream_status(stream)
     checksum = bf.adler32_device(J)
 
-    gpu_id = None
-    try:
-        gpu_id = "GPU-" + str(torch.cuda.get_device_properties(local_rank).uuid)
-    except Exception:
-        gpu_id = None
-    clocks = ClockSampler(gpu_id if rank == 0 else None)
+    clocks = ClockSampler(gpu_uuid(torch, local_rank) if rank == 0 else None)
     if rank == 0:
         clocks.start()
     # keep the GPU busy ~1 s before the timed region so the clock samples cover the load
@@ -336,21 +363,8 @@ def run_ours(args):
     assert bf.adler32_device(J) == checksum
     W.close()
     alg_bytes = d.esize + d.jsize + d.asize + 4 * d.gsize
-    peak, peak_kind = load_peaks()
-    achieved = alg_bytes / (k_ms * 1e-3) / 1e9
-    roofline = {
-        "bound": "hbm",
-        "kernel": "bf_form_beams_tc",
-        "achieved": round(achieved, 1),
-        "peak": peak,
-        "peak_kind": f"{peak_kind} (copy bandwidth)",
-        "unit": "GB/s",
-        "frac": round(achieved / peak, 4),
-        "traffic": profile_traffic(),
-        "algorithmic_bytes": alg_bytes,
-        "kernel_ms": round(k_ms, 4),
-        "tensor_fp8_tflops": round(8 * d.cmacs / (k_ms * 1e-3) / 1e12, 1),
-    }
+    roofline = roofline_of(bf, stream, d.cmacs, alg_bytes, k_ms, "bf_form_beams_tc")
+    roofline["traffic"] = profile_traffic()
 
     e2e = None
     if not args.no_e2e:
@@ -505,7 +519,6 @@ def run_batched(args):
     ms_batch = timed(lambda: batch.run(stream))
     ms_loop = timed(per_problem)
     alg_bytes = sum(d.esize + d.jsize + d.asize + 4 * d.gsize for d, _, _, _ in probs)
-    peak, peak_kind = load_peaks()
     line = {
         "metric": METRIC,
         "value": total_cmac / (ms_batch * 1e-3),
@@ -523,9 +536,7 @@ def run_batched(args):
         "per_problem_launches": {"value": total_cmac / (ms_loop * 1e-3), "ms_per_step": round(ms_loop, 4),
                                  "launches": len(probs)},
         "speedup_vs_per_problem": round(ms_loop / ms_batch, 3),
-        "roofline": {"bound": "hbm", "achieved": round(alg_bytes / (ms_batch * 1e-3) / 1e9, 1), "peak": peak,
-                     "peak_kind": f"{peak_kind} (copy bandwidth)", "unit": "GB/s",
-                     "frac": round(alg_bytes / (ms_batch * 1e-3) / 1e9 / peak, 4)},
+        "roofline": roofline_of(bf, stream, total_cmac, alg_bytes, ms_batch, "bf_form_beams_tc (grouped)"),
         "autotune": batch.info(),
         "parity": "per-problem adler32 of the batched launch equals the per-problem launches",
         "gpu_launches": args.steps,
@@ -696,11 +707,7 @@ def run_served(args):
     served_cfg = {"max_batch": args.max_batch, "max_inflight": args.max_inflight, "spin_wait": not args.no_spin}
     plain_cfg = {"max_batch": 1, "max_inflight": 1, "spin_wait": not args.no_spin}
     out = {}
-    try:
-        gpu_id = "GPU-" + str(torch.cuda.get_device_properties(0).uuid)
-    except Exception:
-        gpu_id = None
-    clocks = ClockSampler(gpu_id)
+    clocks = ClockSampler(gpu_uuid(torch, 0))
     clocks.start()
     for name, cfg in (("served", served_cfg), ("plain", plain_cfg)):
         serve_stream(bf, torch, W, contents, np.zeros(min(200, n)), picks[:200], cfg, args.slots,
@@ -754,6 +761,138 @@ def run_served(args):
     W.close()
 
 
+WIDE = {"ntimes": 16384, "nfrequencies": 16, "ndishes": 1024, "npolarizations": 2, "nbeams": 512, "seed": 4,
+        "refresh_every": 8}
+WIDE_NAME = ("wide array t=16384 f=16 d=1024 p=2 b=512, seed 4; served loop with the weights regenerated every "
+             "8 chunks from seed 4+k")
+
+
+def run_wide(args):
+    """Wide-array chunks through the server (device-resident E and J), the
+    weights refreshed every 8 chunks without a drain; every chunk's adler32
+    against a plain launch with the same weights.  The kernel alone is timed
+    with plain resident launches for the roofline."""
+    import torch
+
+    import beamforming_gb300 as bf
+
+    torch.cuda.set_device(0)
+    w = WIDE
+    d = bf.Dims(w["ntimes"], w["nfrequencies"], w["ndishes"], 2, w["nbeams"])
+    stream = torch.cuda.current_stream()
+    nchunks = args.chunks  # per round; J slots are checked between rounds
+    rounds = args.rounds
+    every = w["refresh_every"]
+    nver = rounds * ((nchunks + every - 1) // every) + 2  # warm-up chunks use version 0
+    NE = 4
+    Es = []
+    for i in range(NE):
+        E = torch.empty(d.esize, dtype=torch.uint8, device="cuda")
+        bf.fill_random_device(E, w["seed"], 2 + i)
+        Es.append(E)
+    G = torch.from_numpy(bf.gains(d)).cuda()
+    As = []
+    for k in range(nver):
+        A = torch.empty(d.asize, dtype=torch.uint8, device="cuda")
+        bf.fill_random_device(A, w["seed"] + k, 1)  # version k: seed 4 + k
+        As.append(A)
+    # expected adler32 of every (version, E) pair: plain resident launches
+    ref = bf.ResidentWeights(d.nfrequencies, d.nbeams, d.ndishes, As[0], G, stream=stream)
+    Jt = torch.empty(d.jsize, dtype=torch.uint8, device="cuda")
+    want = {}
+    for k in range(nver):
+        ref.update(As[k], G, stream=stream)
+        for i in range(NE):
+            ref.form_beams(Jt, Es[i], d.ntimes, stream=stream)
+            bf.stream_status(stream)
+            want[(k, i)] = bf.adler32_device(Jt)
+    # kernel alone (version 0 weights), events around each launch
+    ref.update(As[0], G, stream=stream)
+    for _ in range(3):
+        ref.form_beams(Jt, Es[0], d.ntimes, stream=stream)
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(20)]
+    for n, (a, b) in enumerate(evs):
+        a.record(stream)
+        ref.form_beams(Jt, Es[n % NE], d.ntimes, stream=stream)
+        b.record(stream)
+    torch.cuda.synchronize()
+    bf.stream_status(stream)
+    k_ms = statistics.mean(a.elapsed_time(b) for a, b in evs)
+    alg_bytes = d.esize + d.jsize + d.asize + 4 * d.gsize
+    roofline = roofline_of(bf, stream, d.cmacs, alg_bytes, k_ms, "bf_form_beams_tc")
+    ref.close()
+
+    W = bf.ResidentWeights(d.nfrequencies, d.nbeams, d.ndishes, As[0], G, stream=stream)
+    torch.cuda.synchronize()
+    srv = bf.Server(W, hbm_budget_bytes=1 << 30, max_batch=args.max_batch, max_inflight=args.max_inflight,
+                    spin_wait=not args.no_spin)
+    Js = [torch.empty(d.jsize, dtype=torch.uint8, device="cuda") for _ in range(nchunks)]
+    T = d.ntimes
+
+    def stream_of(n, version0):
+        """Submits n chunks, refreshing the weights every `every` chunks;
+        returns [(ticket, version, E index, J index)]."""
+        out, v = [], version0
+        for i in range(n):
+            if i and i % every == 0:
+                v += 1
+                srv.update_weights(As[v], G)
+            out.append((srv.submit(0, T, Es[i % NE], Js[i], nchannels=d.nfrequencies), v, i % NE, i))
+        return out
+
+    warm = stream_of(min(every, nchunks), 0)
+    srv.drain()
+    for t, *_ in warm:
+        srv.wait(t)
+    clocks = ClockSampler(gpu_uuid(torch, 0))
+    clocks.start()
+    wall, lat, bad, v0 = 0.0, [], 0, 0
+    for _ in range(rounds):
+        v0 += 1
+        srv.update_weights(As[v0], G)
+        t0 = time.perf_counter()
+        subs = stream_of(nchunks, v0)
+        srv.drain()
+        wall += time.perf_counter() - t0
+        v0 = subs[-1][1]
+        lat += [srv.wait(t) for t, *_ in subs]
+        bad += sum(bf.adler32_device(Js[j]) != want[(v, i)] for _, v, i, j in subs)
+    clk = clocks.stop()
+    st = srv.stats()
+    srv.close()
+    W.close()
+    nchunks *= rounds
+    value = nchunks * d.cmacs / wall
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": 1,
+        "steps": nchunks,
+        "warmup": min(every, nchunks),
+        "ms_per_step": round(wall * 1e3 / nchunks, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "int4 complex in, exact integer sums (e4m3 tensor-core operands, f32 accumulate)",
+        "data": "synthetic (seeded uniform 4-bit complex; G from the reference setup() formula)",
+        "config": {"workload": WIDE_NAME, **w, "chunks": nchunks, "buffers": "E and J resident in HBM",
+                   "l2": "E = 537 MB per chunk, larger than L2"},
+        "roofline": roofline,
+        "served": {"weight_updates": st["weight_updates"], "batches": st["batches"],
+                   "max_batch_seen": st["max_batch_seen"],
+                   "latency_ms": {"p50": round(float(np.percentile(lat, 50)) * 1e3, 3),
+                                  "p99": round(float(np.percentile(lat, 99)) * 1e3, 3)},
+                   "kernel_only_value": d.cmacs / (k_ms * 1e-3)},
+        "parity": "every chunk's adler32 equals a plain launch's with the weights current at its submission",
+        "mismatches": int(bad),
+        "clocks": clk,
+        "gpu_launches": st["batches"],
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     if args.workload == "batched":
@@ -761,6 +900,9 @@ def main():
         return
     if args.workload == "served":
         run_served(args)
+        return
+    if args.workload == "wide":
+        run_wide(args)
         return
     if args.frequencies:
         WORKLOAD["nfrequencies"] = args.frequencies

@@ -171,6 +171,13 @@ BF_API int bf_batch_info(const bf_batch *batch, int *ntiles, int *order, int *ws
 
 BF_API int bf_batch_destroy(bf_batch *batch);
 
+/* Measures the dense E4M3 tensor-core rate of the current device, in
+ * TFLOP/s (two flops per multiply-add): every SM issues back-to-back
+ * tcgen05 MMAs of the kind the beamformer uses (M=128, N=256, K=32, A operand
+ * in tensor memory), timed with CUDA events at the run's own clocks.  It is
+ * the tensor roofline the benchmarks report fractions of; takes ~15 ms. */
+BF_API int bf_tensor_peak(double *tflops, bf_stream_t stream);
+
 /* ---------------------------------------------------------------- serving */
 
 /* A served stream of voltage chunks with continuous batching.  No
@@ -178,8 +185,9 @@ BF_API int bf_batch_destroy(bf_batch *batch);
  * a fixed HBM pool has room for their buffers, packs them into one grouped
  * tensor-core launch, and keeps up to max_inflight launches in flight, so
  * chunks that arrive while others run are admitted as memory and launch slots
- * free up.  The resident weights must not be updated while chunks are in
- * flight (drain first). */
+ * free up.  The caller's resident weights must not be updated while chunks
+ * are in flight (drain first); bf_server_update_weights refreshes the
+ * server's weights without a drain. */
 typedef struct bf_server bf_server;
 
 typedef struct bf_server_config {
@@ -194,6 +202,7 @@ typedef struct bf_server_stats {
   int64_t submitted, completed;
   int64_t batches, chunks_launched, max_batch_seen;
   int64_t pool_bytes, pool_peak_bytes;
+  int64_t weight_updates;
 } bf_server_stats;
 
 /* Creates a server over resident weights (all channels = the weights' frequencies). */
@@ -205,6 +214,15 @@ BF_API int bf_server_create(bf_server **out, const bf_weights *weights, const bf
  * arrival time is now.  Needs ntimes % 16 == 0. */
 BF_API int bf_server_submit(bf_server *server, int channel, int nchannels, int64_t ntimes, const uint8_t *E,
                             int e_on_device, uint8_t *J, int j_on_device, int64_t *ticket);
+
+/* Refreshes the weights (A[f][b][d], G[f][b] for all of the server's channels,
+ * host or device memory per ptr_kind) without draining: chunks submitted
+ * after this call use the new weights, chunks submitted before it keep the
+ * weights they were submitted under.  The server keeps up to three refreshed
+ * versions besides the caller's own weights (which it never writes); the call
+ * waits only while every version still has chunks on it.  A and G may be
+ * reused when it returns. */
+BF_API int bf_server_update_weights(bf_server *server, const uint8_t *A, const float *G, int ptr_kind);
 
 /* Blocks until the ticket's chunk is complete (J written); returns its latency
  * (submission to completion) in seconds. */
