@@ -67,7 +67,7 @@ struct DeviceCtx {
   int *err = nullptr;       // device error word written by kernels
   uint32_t *adler = nullptr;  // device adler32 result
   DevBuf E, A, G, J;        // staging for host-pointer calls
-  DevBuf W, bias;           // tensor-core operand for non-resident calls
+  DevBuf W, dig;            // tensor-core operand for non-resident calls
   DevBuf partials;          // adler32 partial sums
 };
 
@@ -125,7 +125,7 @@ void plan_weights(TcWeights &w, int64_t F, int64_t B, int64_t D) {
 }
 
 size_t weights_bytes(const TcWeights &w) { return static_cast<size_t>(w.F) * w.nw * 2 * w.D; }
-size_t bias_bytes(const TcWeights &w) { return static_cast<size_t>(w.F) * w.nw_pad * sizeof(float); }
+size_t digit_bytes(const TcWeights &w) { return static_cast<size_t>(w.F) * w.nw_pad * kDigitRow; }
 
 int choose_tensor(const bf_dims &d, bool *use_tc) {
   const int k = g_kernel.load();
@@ -137,18 +137,18 @@ int choose_tensor(const bf_dims &d, bool *use_tc) {
   return BF_OK;
 }
 
-// All four arrays on the device; the tensor-core operand goes to W / bias.
+// All four arrays on the device; the tensor-core operand goes to W / dig.
 int run_device_bufs(const bf_dims &d, uint8_t *J, const uint8_t *E, const uint8_t *A, const float *G, DevBuf &W,
-                    DevBuf &bias, int *err, cudaStream_t s);
+                    DevBuf &dig, int *err, cudaStream_t s);
 
 // All four arrays on the device.  Operand scratch comes from ctx (caller holds ctx.mu).
 int run_device(DeviceCtx &c, const bf_dims &d, uint8_t *J, const uint8_t *E, const uint8_t *A, const float *G,
                cudaStream_t s) {
-  return run_device_bufs(d, J, E, A, G, c.W, c.bias, c.err, s);
+  return run_device_bufs(d, J, E, A, G, c.W, c.dig, c.err, s);
 }
 
 int run_device_bufs(const bf_dims &d, uint8_t *J, const uint8_t *E, const uint8_t *A, const float *G, DevBuf &Wb,
-                    DevBuf &biasb, int *err, cudaStream_t s) {
+                    DevBuf &digb, int *err, cudaStream_t s) {
   if (jsize(d) == 0) return BF_OK;
   bool use_tc = false;
   const int st = choose_tensor(d, &use_tc);
@@ -164,9 +164,9 @@ int run_device_bufs(const bf_dims &d, uint8_t *J, const uint8_t *E, const uint8_
   TcWeights w;
   plan_weights(w, d.nfrequencies, d.nbeams, d.ndishes);
   BF_TRY(Wb.reserve(weights_bytes(w)));
-  BF_TRY(biasb.reserve(bias_bytes(w)));
+  BF_TRY(digb.reserve(digit_bytes(w)));
   w.W = Wb.as<uint8_t>();
-  w.bias = biasb.as<float>();
+  w.dig = digb.as<uint8_t>();
   w.G = G;
   BF_TRY(launch_prep_weights(w, A, s));
   t_last_kernel = "tensor";
@@ -229,9 +229,9 @@ int run_host_pipelined(DeviceCtx &c, const bf_dims &d, uint8_t *J, const uint8_t
   if (use_tc) {
     plan_weights(w, d.nfrequencies, d.nbeams, d.ndishes);
     BF_TRY(c.W.reserve(weights_bytes(w)));
-    BF_TRY(c.bias.reserve(bias_bytes(w)));
+    BF_TRY(c.dig.reserve(digit_bytes(w)));
     w.W = c.W.as<uint8_t>();
-    w.bias = c.bias.as<float>();
+    w.dig = c.dig.as<uint8_t>();
     w.G = c.G.as<float>();
     BF_TRY(launch_prep_weights(w, c.A.as<uint8_t>(), l0.s));
   }
@@ -383,7 +383,7 @@ int bf_weights_create(bf_weights **out, int64_t nfrequencies, int64_t nbeams, in
   cudaError_t e = cudaMalloc(&w->A, na);
   if (e == cudaSuccess) e = cudaMalloc(&w->G, ng * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&w->tc.W, weights_bytes(w->tc));
-  if (e == cudaSuccess) e = cudaMalloc(&w->tc.bias, bias_bytes(w->tc));
+  if (e == cudaSuccess) e = cudaMalloc(&w->tc.dig, digit_bytes(w->tc));
   if (e != cudaSuccess) {
     bf_weights_destroy(w);
     return to_status(e);
@@ -417,7 +417,7 @@ int bf_weights_destroy(bf_weights *w) {
   if (w->A) cudaFree(w->A);
   if (w->G) cudaFree(w->G);
   if (w->tc.W) cudaFree(w->tc.W);
-  if (w->tc.bias) cudaFree(w->tc.bias);
+  if (w->tc.dig) cudaFree(w->tc.dig);
   delete w;
   return BF_OK;
 }

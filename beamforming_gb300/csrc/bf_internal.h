@@ -17,16 +17,18 @@ cudaError_t launch_simt(const bf_dims &d, uint8_t *J, const uint8_t *E, const ui
 
 // Tensor-core path ------------------------------------------------------------
 
-// Layout of the resident operand built from A: for each frequency, nw_pad
-// rows of 2*D bytes (E4M3 values), and a float bias per row.
+// Layout of the resident operand built from A: for each frequency, nw rows of
+// 2*D bytes (E4M3 values), and per row a 32-byte row of E4M3 digits of the
+// offset correction sum_k W[n][k] (the operand of one extra MMA per tile).
+constexpr int kDigitRow = 32;  // bytes per digit row
 struct TcWeights {
   int64_t F = 0, B = 0, D = 0;
   int nb_pass = 0;   // beams per tensor-core pass (multiple of 8, <= 128)
   int npass = 0;     // passes over the beams
   int nw = 0;        // W rows per frequency holding data: 2 * roundup(B, 8)
-  int nw_pad = 0;    // bias rows per frequency: npass * 2 * nb_pass
+  int nw_pad = 0;    // digit rows per frequency: npass * 2 * nb_pass
   uint8_t *W = nullptr;      // [F][nw][2D]
-  float *bias = nullptr;     // [F][nw_pad]
+  uint8_t *dig = nullptr;    // [F][nw_pad][kDigitRow]
   const float *G = nullptr;  // [F][B] (device)
 };
 
@@ -36,7 +38,7 @@ bool tc_supported(const bf_dims &d);
 // Beams per pass and number of passes for B beams.
 void tc_plan_beams(int64_t B, int *nb_pass, int *npass);
 
-// Fills w.W and w.bias from device A (w's sizes and buffers already set).
+// Fills w.W and w.dig from device A (w's sizes and buffers already set).
 cudaError_t launch_prep_weights(const TcWeights &w, const uint8_t *A, cudaStream_t s);
 
 // Beamforms T times of device E into device J with prepared weights.  `err`
@@ -49,18 +51,18 @@ cudaError_t launch_tc(const TcWeights &w, int64_t T, uint8_t *J, const uint8_t *
 // One beamforming problem of a tensor-core launch: operand descriptors,
 // pointers, shape.  A plain launch carries one inline; a grouped launch reads
 // an array of them from device memory, ordered by tile_begin.
-struct alignas(64) TcProblem {
+struct TcProblem {  // 128-byte aligned through its tensor maps
   CUtensorMap tm_e;  // E[t][f][d*p] bytes: dims {2D, F, T}, box {128, 1, 64}, 128B swizzle
   CUtensorMap tm_w;  // W[f][n][k] bytes: dims {2D, nw, F}, box {128, 2*nb_pass, 1}, 128B swizzle
+  CUtensorMap tm_d;  // digits[f][n][32] bytes: dims {32, nw_pad, F}, box {32, 2*nb_pass, 1}, 32B swizzle
   uint8_t *J;
   const float *G;
-  const float *bias;
   int64_t jpitch;    // bytes between consecutive (b, f, p) rows of J
   int T, F, B;
   int nb_pass;       // beams per pass
   int npass;
   int ntt;           // time tiles per frequency
-  int nw_pad;        // bias entries per frequency
+  int nw_pad;        // digit rows per frequency
   int tile_begin;    // first tile of this problem in the launch
 };
 

@@ -6,13 +6,13 @@
 // allocate afterwards (an allocation can block or fail mid-stream), or a host
 // framework that owns the device memory pool and forbids other allocators.
 // The regular entry points keep their scratch (the prepared E4M3 operand W,
-// its row sums and the device error word) in buffers the library allocates on
+// the digit rows of its row sums and the device error word) in buffers the library allocates on
 // first use.  This entry point keeps that scratch in one fixed array in
 // device memory instead, reserved when the library is loaded:
 //
 //   g_noalloc_scratch   kNoAllocScratchBytes = 4 MiB, 256-byte aligned
 //     [0, 256)                    device error word (cleared every call)
-//     [256, 256 + bias bytes)     bias[f][n]   float, F * npass * 2 * nb_pass
+//     [256, 256 + digit bytes)    dig[f][n][32] E4M3, F * npass * 2 * nb_pass * 32
 //     [.., .. + W bytes)          W[f][n][k]   E4M3,  F * 2 * roundup(B, 8) * 2 * D
 //
 // Every GPU that loads the library holds these 4 MiB until the process exits.
@@ -84,9 +84,9 @@ extern "C" int bf_form_beams_noalloc(const bf_dims *dims, uint8_t *J, const uint
   tc_plan_beams(d.nbeams, &w.nb_pass, &w.npass);
   w.nw = static_cast<int>((d.nbeams + 7) / 8 * 8 * 2);
   w.nw_pad = w.npass * 2 * w.nb_pass;
-  const size_t bias_bytes = static_cast<size_t>(w.F) * w.nw_pad * sizeof(float);
+  const size_t dig_bytes = static_cast<size_t>(w.F) * w.nw_pad * kDigitRow;
   const size_t w_bytes = static_cast<size_t>(w.F) * w.nw * 2 * w.D;
-  if (kErrBytes + round256(bias_bytes) + w_bytes > kNoAllocScratchBytes) return BF_ERR_TOO_LARGE;
+  if (kErrBytes + round256(dig_bytes) + w_bytes > kNoAllocScratchBytes) return BF_ERR_TOO_LARGE;
 
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
@@ -97,12 +97,12 @@ extern "C" int bf_form_beams_noalloc(const bf_dims *dims, uint8_t *J, const uint
   if (e != cudaSuccess) return status_of(e);
   uint8_t *scratch = static_cast<uint8_t *>(base);
   int *err = reinterpret_cast<int *>(scratch);
-  w.bias = reinterpret_cast<float *>(scratch + kErrBytes);
-  w.W = scratch + kErrBytes + round256(bias_bytes);
+  w.dig = scratch + kErrBytes;
+  w.W = scratch + kErrBytes + round256(dig_bytes);
   w.G = G;
 
   // The array keeps the previous call's contents: the error word must start at
-  // zero; W and bias are rewritten in full below.
+  // zero; W and the digit rows are rewritten in full below.
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   e = cudaMemsetAsync(err, 0, sizeof(int), s);
   if (e == cudaSuccess) e = launch_prep_weights(w, A, s);

@@ -220,6 +220,16 @@ __device__ __forceinline__ void tmem_st_32x32b_x32(uint32_t taddr, const uint32_
       : "memory");
 }
 
+// 32 lanes x 16 consecutive 32-bit columns from registers: thread i writes lane (base + i).
+__device__ __forceinline__ void tmem_st_32x32b_x16(uint32_t taddr, const uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+      "{%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16};" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]),
+      "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
+      : "memory");
+}
+
 __device__ __forceinline__ void tmem_st_wait() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 // Arrive once on an mbarrier when every tcgen05 operation this thread issued
@@ -260,6 +270,18 @@ __device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
   d |= static_cast<uint64_t>((1024u >> 4) & 0x3FFFu) << 32;  // stride byte offset: next 8-row group
   d |= static_cast<uint64_t>(1u) << 46;                     // descriptor version
   d |= static_cast<uint64_t>(2u) << 61;                     // 128-byte swizzle
+  return d;
+}
+
+// Shared-memory matrix descriptor for a K-major operand whose rows are 32
+// bytes in the 32-byte swizzle the TMA writes (8-row groups of 256 bytes).
+__device__ __forceinline__ uint64_t smem_desc_sw32(uint32_t addr) {
+  uint64_t d = 0;
+  d |= static_cast<uint64_t>((addr >> 4) & 0x3FFFu);       // start address
+  d |= static_cast<uint64_t>(1u) << 16;                    // leading byte offset (unused for this layout)
+  d |= static_cast<uint64_t>((256u >> 4) & 0x3FFFu) << 32;  // stride byte offset: next 8-row group
+  d |= static_cast<uint64_t>(1u) << 46;                    // descriptor version
+  d |= static_cast<uint64_t>(6u) << 61;                    // 32-byte swizzle
   return d;
 }
 

@@ -163,7 +163,7 @@ TcWeights channel_view(const TcWeights &w, int c0, int n) {
   TcWeights v = w;
   v.F = n;
   v.W = w.W + static_cast<int64_t>(c0) * w.nw * 2 * w.D;
-  v.bias = w.bias + static_cast<int64_t>(c0) * w.nw_pad;
+  v.dig = w.dig + static_cast<int64_t>(c0) * w.nw_pad * kDigitRow;
   v.G = w.G + static_cast<int64_t>(c0) * w.B;
   return v;
 }

@@ -13,29 +13,33 @@
 // [0, 15] is, read as E4M3, exactly u * 2^-9 (exponent field 0 or 1: the
 // subnormal and the first normal binade share the step 2^-9).  So the raw
 // ucomplex4 nibbles (value x stored as u = x + 8) become tensor-core operands
-// with one AND per 4 values; the offset is removed in the epilogue:
+// with one AND per 4 values.  The offset goes into the accumulator's start
+// value, which the epilogue writes before handing the accumulator over:
 //
-//   sum_k (u_k - 8) W[n][k] = 512 * acc[n] - 8 * sum_k W[n][k]
+//   acc[n] = -8 * sum_k W[n][k] / 512 + sum_k u_k W[n][k] / 512
+//          = sum_k (u_k - 8) W[n][k] / 512 = raw / 512
 //
-// W holds the integers Ar, -Ai, Ai in [-8, 8], exact in E4M3; every product
-// and every partial sum is an integer multiple of 2^-9 below 2^8 in
-// magnitude (17 significant bits), exact in the f32 accumulator.  The
-// requantisation clamp(lrint(G * float(raw)), -7, 7) of cpu.cxx:37-39 runs in
-// the epilogue with one IEEE multiply and a round-half-even conversion.
+// W holds the integers Ar, -Ai, Ai in [-8, 8], exact in E4M3; the start value
+// and every partial sum are integer multiples of 2^-9 below 2^10 in magnitude
+// (at most 19 significant bits), exact in the f32 accumulator.  The
+// requantisation clamp(lrint(G * float(raw)), -7, 7) of cpu.cxx:37-39 is one
+// IEEE multiply by 512 G (exactly G * raw) and a round-half-even conversion.
 //
-// Warp roles (one 608-thread CTA per SM, persistent over tiles):
+// Warp roles (one CTA per SM, persistent over tiles; warp numbers for the
+// default layout of 8 epilogue warps and 2 unpack groups, 608 threads):
 //   warps 0-7    epilogue: TMEM accumulator -> registers -> requantise -> 4x4 byte
-//                transpose across lanes -> 32-bit stores of 4 consecutive times of one beam
+//                transpose across lanes -> 32-bit stores of 4 consecutive times of
+//                one beam; then the start values of the accumulator's next tile
 //   warp  8      E producer: TMA of raw E boxes into a deep ring released by the unpack
 //   warp  9      TMEM allocator and single-thread MMA issuer (A operand from TMEM)
 //   warp  10     W producer: TMA of the W slice of each K stage, released by the MMA
-//   warps 11-18  unpack, two groups of four taking alternate K stages: raw E bytes ->
+//   warps 11-18  unpack, groups of four taking K stages in turn: raw E bytes ->
 //                de-interleaved E4M3 operand rows written straight into tensor memory
 //                (tcgen05.st); no shared-memory operand
 //
 // GEMM row r of a tile (TMEM lane r) is (t, p) = (r / 2, r % 2) for the 64 times
 // of the tile.  TMEM columns: accumulators at [0, N) and [256, 256 + N), unpacked
-// E stages (32 columns = 128 K bytes each) in the remaining columns.
+// E stages (64 columns = 256 K bytes each) in the remaining columns.
 #include "bf_internal.h"
 #include "bf_ptx.cuh"
 
@@ -48,12 +52,19 @@
 namespace bf {
 namespace {
 
-constexpr int kThreads = 608;
-constexpr int kEpiThreads = 256;        // warps 0-7
-constexpr int kEProdWarp = 8;
-constexpr int kMmaWarp = 9;
-constexpr int kWProdWarp = 10;
-constexpr int kUnpackWarp0 = 11;        // warps 11-18: two groups, each covering TMEM lane quarters 3, 0, 1, 2
+// Warp layout: kEpiWarps epilogue warps, the three single-thread roles, then
+// kUnpackGroups groups of four unpack warps.  A warp reaches TMEM lanes
+// 32 * (warp % 4) .. + 31 only, so every role that touches TMEM rows comes in
+// fours covering the four lane quarters.
+constexpr int kEpiWarps = 8;
+constexpr int kUnpackGroups = 1;
+constexpr int kEpiThreads = 32 * kEpiWarps;
+constexpr int kEpiParts = kEpiWarps / 4;  // column parts: each is read by four warps (one per lane quarter)
+constexpr int kEProdWarp = kEpiWarps;
+constexpr int kMmaWarp = kEpiWarps + 1;
+constexpr int kWProdWarp = kEpiWarps + 2;
+constexpr int kUnpackWarp0 = kEpiWarps + 3;
+constexpr int kThreads = 32 * (kUnpackWarp0 + 4 * kUnpackGroups);
 constexpr int kTT = 64;                 // times per tile
 constexpr int kBM = 128;                // GEMM rows per tile
 constexpr int kKC = 128;                // K bytes per TMA box / swizzle atom (64 dishes x re/im)
@@ -65,6 +76,16 @@ constexpr int kAccCols = 256;           // TMEM column offset of the second accu
 constexpr int kStageCols = kStageK / 4;  // TMEM columns per unpacked stage
 constexpr int kSmemLimit = 232448;      // 227 KiB opt-in per block
 constexpr int kMaxStages = 8;
+constexpr int kDigSlots = 2;            // digit-row slots (one per tile in flight)
+// Offset correction: one extra MMA per tile, issued first (it also clears the
+// accumulator), multiplies a constant A tile by the tile's digit rows.  The
+// constant row holds -2^-6, -2^-2, -4, -64, -256 at K = 0..4 (again at 16..20,
+// so the 32-byte swizzle cannot move them), the digit row of n holds d0..d3 and
+// 4 d4 with sum_k W[n][k] = d0 + 16 d1 + 256 d2 + 4096 d3 + 65536 d4, so the
+// accumulator starts at -sum_k W[n][k] / 64 = -8 sum_k W[n][k] / 512 exactly.
+constexpr uint32_t kDigitScaleLo = 0xE8C8A888u;  // E4M3 -2^-6, -2^-2, -4, -64
+constexpr uint32_t kDigitScaleHi = 0x000000F8u;  // E4M3 -256
+constexpr int kConstABytes = kBM * kDigitRow;
 constexpr int kMaxWSlots = 6;
 constexpr int kMinRaw = 4;
 constexpr int kMaxRaw = 16;
@@ -102,21 +123,25 @@ __device__ __forceinline__ const TcProblem &problem_of(const TcParams &p, int ti
 }
 
 struct SmemPlan {
-  int wbox, wbytes;
-  int off_w, off_r, off_g, off_bar, nbar, total;
+  int wbox, wbytes, dbytes;
+  int off_w, off_a, off_d, off_r, off_g, off_bar, nbar, total;
 };
 
 __host__ __device__ inline SmemPlan smem_plan(int stages, int wslots, int raw, int nb_pass) {
   SmemPlan s{};
   s.wbox = 2 * nb_pass * kKC;
   s.wbytes = kSub * s.wbox;
+  s.dbytes = (2 * nb_pass * kDigitRow + 1023) / 1024 * 1024;
   s.off_w = 0;
-  s.off_r = s.off_w + wslots * s.wbytes;
-  // two buffers of gains [nb_pass] + row sums [2 * nb_pass]: this tile's and the next tile's
+  s.off_a = s.off_w + wslots * s.wbytes;  // constant A tile of the offset MMA
+  s.off_d = s.off_a + kConstABytes;       // digit-row slots
+  s.off_r = s.off_d + kDigSlots * s.dbytes;
+  // two gain entries (this tile's and the next tile's): 512 * G [nb_pass]
   s.off_g = s.off_r + raw * kRawBytes;
-  s.off_bar = s.off_g + 2 * 3 * nb_pass * 4;
-  // raw_full[R], raw_empty[R], w_full[SW], w_empty[SW], a_full[S], empty[S], accfull[2], accempty[2]
-  s.nbar = 2 * raw + 2 * wslots + 2 * stages + 4;
+  s.off_bar = s.off_g + 2 * nb_pass * 4;
+  // raw_full[R], raw_empty[R], w_full[SW], w_empty[SW], a_full[S], empty[S], accfull[2], accempty[2],
+  // d_full[2], d_empty[2]
+  s.nbar = 2 * raw + 2 * wslots + 2 * stages + 4 + 2 * kDigSlots;
   s.total = s.off_bar + 8 * s.nbar + 16;
   return s;
 }
@@ -157,6 +182,8 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
   const int S = p.stages, SW = p.wslots, R = p.raw;
   const SmemPlan sp = smem_plan(S, SW, R, p.max_nb_pass);
   uint8_t *sW = smem + sp.off_w;
+  uint8_t *sA = smem + sp.off_a;
+  uint8_t *sD = smem + sp.off_d;
   uint8_t *sR = smem + sp.off_r;
   float *sG = reinterpret_cast<float *>(smem + sp.off_g);
   const uint32_t bar0 = smem_u32(smem + sp.off_bar);
@@ -168,6 +195,8 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
   auto empty = [&](int s) { return bar0 + 8u * (2 * R + 2 * SW + S + s); };
   auto accfull = [&](int i) { return bar0 + 8u * (2 * R + 2 * SW + 2 * S + i); };
   auto accempty = [&](int i) { return bar0 + 8u * (2 * R + 2 * SW + 2 * S + 2 + i); };
+  auto d_full = [&](int i) { return bar0 + 8u * (2 * R + 2 * SW + 2 * S + 4 + i); };
+  auto d_empty = [&](int i) { return bar0 + 8u * (2 * R + 2 * SW + 2 * S + 4 + kDigSlots + i); };
   uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(smem + sp.off_bar + 8 * sp.nbar);
 
   const int warp = threadIdx.x >> 5;
@@ -192,8 +221,19 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
       mbar_init(accfull(i), 1);
       mbar_init(accempty(i), kEpiThreads);
     }
+    for (int i = 0; i < kDigSlots; ++i) {
+      mbar_init(d_full(i), 1);
+      mbar_init(d_empty(i), 1);
+    }
     fence_barrier_init();
   }
+  // constant A tile of the offset MMA: every row the same, so the 32-byte
+  // swizzle leaves it unchanged
+  for (int i = threadIdx.x; i < kConstABytes / 4; i += blockDim.x) {
+    const int w = i & 7;
+    reinterpret_cast<uint32_t *>(sA)[i] = (w == 0 || w == 4) ? kDigitScaleLo : (w == 1 || w == 5) ? kDigitScaleHi : 0u;
+  }
+  fence_proxy_async_smem();
   if (warp == kMmaWarp) {
     tmem_alloc(smem_u32(tmem_holder), 2 * kAccCols);
     tmem_relinquish();
@@ -242,8 +282,8 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
     // ------------------------------------------------------------ W producer
     if (lane == 0 && !p.test_stall) {
       const uint64_t pol_w = policy_evict_last();
-      Ring wr(SW);
-      uint32_t it = 0;
+      Ring wr(SW), dr(kDigSlots);
+      uint32_t it = 0, dit = 0;
       bool ok = true;
       for (int tile = blockIdx.x; ok && tile < p.ntiles; tile += gridDim.x) {
         int lt;
@@ -251,6 +291,17 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
         const int pass = lt % P.npass;
         const int f = lt / (P.npass * P.ntt);
         const int wbox = 2 * P.nb_pass * kKC;
+        {  // the tile's digit rows, for the offset MMA
+          const int ds = static_cast<int>(dr.idx);
+          if (!mbar_wait(d_empty(ds), dr.phase ^ 1u, err, kDevTimeoutEmpty)) {
+            ok = false;
+            break;
+          }
+          mbar_arrive_expect_tx(d_full(ds), 2 * P.nb_pass * kDigitRow);
+          tma_load_3d(smem_u32(sD + ds * sp.dbytes), &P.tm_d, d_full(ds), 0, pass * 2 * P.nb_pass, f, pol_w);
+          dr.advance();
+          ++dit;
+        }
         for (int ks = 0; ks < p.nk; ++ks, ++it, wr.advance()) {
           const int s = static_cast<int>(wr.idx);
           if (!mbar_wait(w_empty(s), wr.phase ^ 1u, err, kDevTimeoutEmpty)) {
@@ -267,12 +318,15 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
       if (!ok) {
         for (uint32_t k = (it >= static_cast<uint32_t>(SW) ? it - SW : 0); k < it; ++k)
           mbar_wait(w_full(static_cast<int>(k % SW)), (k / SW) & 1u, err, kDevTimeoutFull);
+        for (uint32_t k = (dit >= static_cast<uint32_t>(kDigSlots) ? dit - kDigSlots : 0); k < dit; ++k)
+          mbar_wait(d_full(static_cast<int>(k % kDigSlots)), (k / kDigSlots) & 1u, err, kDevTimeoutFull);
       }
     }
   } else if (warp == kMmaWarp) {
     // ------------------------------------------------------------ MMA issuer
     if (lane == 0) {
-      Ring ar(S), wr(SW);
+      Ring ar(S), wr(SW), dr(kDigSlots);
+      const uint64_t a_const = smem_desc_sw32(smem_u32(sA));
       uint32_t local = 0;
       bool ok = true;
       for (int tile = blockIdx.x; ok && tile < p.ntiles; tile += gridDim.x, ++local) {
@@ -283,8 +337,14 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
         const uint32_t ab = local & 1u;
         const uint32_t aph = (local >> 1) & 1u;
         if (!mbar_wait(accempty(ab), aph ^ 1u, err, kDevTimeoutAccEmpty)) break;
+        const int ds = static_cast<int>(dr.idx);
+        if (!mbar_wait(d_full(ds), dr.phase, err, kDevTimeoutFull)) break;
         tc_fence_after();
         const uint32_t d_tmem = tmem_base + ab * kAccCols;
+        // the offset MMA starts the accumulator at -8 sum_k W[n][k] / 512
+        mma_f8f6f4(d_tmem, a_const, smem_desc_sw32(smem_u32(sD + ds * sp.dbytes)), idesc, 0u);
+        mma_commit(d_empty(ds));
+        dr.advance();
         for (int ks = 0; ks < p.nk; ++ks, ar.advance(), wr.advance()) {
           const int s = static_cast<int>(ar.idx);
           const int sw = static_cast<int>(wr.idx);
@@ -300,7 +360,7 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
           for (int kk = 0; kk < kStageK / 32; ++kk) {
             // K step kk: box kk / 4, 32 bytes into its 128-byte rows (descriptor address field is in 16 B units)
             const uint64_t off = static_cast<uint64_t>(((kk >> 2) * wbox + 32 * (kk & 3)) >> 4);
-            mma_f8f6f4_ts(d_tmem, a_tmem + 8 * kk, b_desc + off, idesc, (ks | kk) != 0 ? 1u : 0u);
+            mma_f8f6f4_ts(d_tmem, a_tmem + 8 * kk, b_desc + off, idesc, 1u);
           }
           mma_commit(empty(s));
           mma_commit(w_empty(sw));
@@ -311,8 +371,8 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
     }
   } else if (warp >= kUnpackWarp0) {
     // ------------------------------------------------------------ unpack
-    // Group g (warps 11-14 or 15-18) takes the K stages with it % 2 == g.  Lane
-    // pair (2u, 2u+1) of quarter q holds rows (t, p=0) and (t, p=1) of time
+    // Group g takes the K stages with it % kUnpackGroups == g.  Lane pair
+    // (2u, 2u+1) of quarter q holds rows (t, p=0) and (t, p=1) of time
     // t = 16q + u: both lanes read the raw row and keep their polarization.
     const int group = (warp - kUnpackWarp0) >> 2;
     const int q = warp & 3;
@@ -320,17 +380,17 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
     const uint32_t tl = 16u * q + (lane >> 1);
     const uint32_t lane_addr = static_cast<uint32_t>(32 * q) << 16;
     const uint32_t sel = pp ? 0x7531u : 0x6420u;  // odd or even bytes: polarization 1 or 0
-    // this CTA's K stages: tiles blockIdx.x, blockIdx.x + gridDim.x, ... times nk; group g takes every other
+    // this CTA's K stages: tiles blockIdx.x, blockIdx.x + gridDim.x, ... times nk
     const uint32_t my_tiles =
         static_cast<int>(blockIdx.x) < p.ntiles ? (p.ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0u;
     const uint32_t total = my_tiles * static_cast<uint32_t>(p.nk);
     Ring rr(R), ar(S);
-    if (group) {
+    for (int g = 0; g < group; ++g) {
       rr.advance();
       ar.advance();
     }
     bool ok = true;
-    for (uint32_t it = group; ok && it < total; it += 2, rr.advance(), rr.advance(), ar.advance(), ar.advance()) {
+    for (uint32_t it = group; ok && it < total; it += kUnpackGroups) {
       {
         const int r = static_cast<int>(rr.idx);
         const int s = static_cast<int>(ar.idx);
@@ -374,13 +434,18 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
         tc_fence_before();
         mbar_arrive(a_full(s));
       }
+#pragma unroll
+      for (int g = 0; g < kUnpackGroups; ++g) {
+        rr.advance();
+        ar.advance();
+      }
     }
   } else {
     // ------------------------------------------------------------ epilogue
     // Warp w reads TMEM lane quarter w % 4 (times 16q..16q+15, both
-    // polarizations interleaved by lane) and column half w / 4.
+    // polarizations interleaved by lane) and column part w / 4.
     const int q = warp & 3;
-    const int half = warp >> 2;
+    const int part = warp >> 2;
     const uint32_t pol = lane & 1u;
     const uint32_t lane_addr = static_cast<uint32_t>(32 * q) << 16;
     const uint32_t j4 = (lane >> 1) & 3u;  // position among the 4 lanes of equal polarization
@@ -388,19 +453,20 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
     // byte-transpose selectors: 4 lanes x 4 beams -> each lane holds one beam's 4 times
     const uint32_t sel1 = (j4 & 1) ? 0x3715u : 0x6240u;
     const uint32_t sel2 = (j4 & 2) ? 0x3276u : 0x5410u;
-    const int gstride = 3 * p.max_nb_pass;  // floats per gain buffer
+    const int gstride = p.max_nb_pass;  // floats per gain entry
     const float kMagic = 12582920.0f;  // 1.5 * 2^23 + 8: x + kMagic has rint(x) + 8 in its low mantissa bits
 
-    // gains [nb_pass] and row sums [2 * nb_pass] of a tile's (frequency, beam pass): value i
+    // Gain entry of a tile's (frequency, beam pass): 512 * G[b0 + i].  The
+    // accumulator ends at raw / 512 exactly, and the power-of-two scaling is
+    // exact, so (512 G) * (raw / 512) rounds like G * raw (cpu.cxx:37).
     auto gain_value = [&](int tile, int i) -> float {
       int lt;
       const TcProblem &Q = problem_of<kGrouped>(p, tile, lt);
-      if (i >= 3 * Q.nb_pass) return 0.0f;
+      if (i >= Q.nb_pass) return 0.0f;
       const int pass = lt % Q.npass;
       const int f = lt / (Q.npass * Q.ntt);
       const int b0 = pass * Q.nb_pass;
-      if (i < Q.nb_pass) return (b0 + i < Q.B) ? __ldg(Q.G + static_cast<int64_t>(f) * Q.B + b0 + i) : 0.0f;
-      return __ldg(Q.bias + static_cast<int64_t>(f) * Q.nw_pad + 2 * b0 + (i - Q.nb_pass));
+      return (b0 + i < Q.B) ? 512.0f * __ldg(Q.G + static_cast<int64_t>(f) * Q.B + b0 + i) : 0.0f;
     };
     if (static_cast<int>(blockIdx.x) < p.ntiles)
       for (int i = threadIdx.x; i < gstride; i += kEpiThreads) sG[i] = gain_value(blockIdx.x, i);
@@ -413,8 +479,7 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
       const int tt = (lt / P.npass) % P.ntt;
       const int f = lt / (P.npass * P.ntt);
       const int nchunk = P.nb_pass / 8;
-      const int c_mid = (nchunk + 1) / 2;
-      const int c_begin = half ? c_mid : 0, c_end = half ? nchunk : c_mid;
+      const int c_begin = part * nchunk / kEpiParts, c_end = (part + 1) * nchunk / kEpiParts;
       const uint32_t ab = local & 1u;
       const uint32_t aph = (local >> 1) & 1u;
       const int b0 = pass * P.nb_pass;
@@ -430,33 +495,29 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
         if (next < p.ntiles && i < gstride) pre[k] = gain_value(next, i);
       }
       const bool got = mbar_wait(accfull(ab), aph, err, kDevTimeoutAccFull);
-      if (!named_bar_and(2, kEpiThreads, got)) break;  // all eight warps leave together
+      if (!named_bar_and(2, kEpiThreads, got)) break;  // all epilogue warps leave together
       tc_fence_after();
       const int64_t t = static_cast<int64_t>(tt) * kTT + 16 * q + 4 * g4;  // first of this lane's 4 times
       const bool t_ok = t < P.T;
       const uint32_t acc_addr = tmem_base + ab * kAccCols + lane_addr;
+      // J[b][f][p][t..t+3] (Jlinear, arraysizes.hxx:92) of beam b0 + j4; beams are bstride bytes apart
+      const int64_t bstride = static_cast<int64_t>(P.F) * 2 * P.jpitch;
+      uint8_t *const jrow =
+          P.J + ((static_cast<int64_t>(b0 + static_cast<int>(j4)) * P.F + f) * 2 + pol) * P.jpitch + t;
+      const int blim = P.B - b0 - static_cast<int>(j4);  // beam offsets below this exist
 
       auto process = [&](int c, const uint32_t (&r)[16]) {
         const float4 ga = *reinterpret_cast<const float4 *>(gcur + 8 * c);
         const float4 gb = *reinterpret_cast<const float4 *>(gcur + 8 * c + 4);
-        const float *bs = gcur + P.nb_pass + 16 * c;
-        const float4 bra = *reinterpret_cast<const float4 *>(bs);
-        const float4 brb = *reinterpret_cast<const float4 *>(bs + 4);
-        const float4 bia = *reinterpret_cast<const float4 *>(bs + 8);
-        const float4 bib = *reinterpret_cast<const float4 *>(bs + 12);
         const float gv[8] = {ga.x, ga.y, ga.z, ga.w, gb.x, gb.y, gb.z, gb.w};
-        const float br[8] = {bra.x, bra.y, bra.z, bra.w, brb.x, brb.y, brb.z, brb.w};
-        const float bi[8] = {bia.x, bia.y, bia.z, bia.w, bib.x, bib.y, bib.z, bib.w};
         uint32_t qre[8], qim[8];
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
-          // raw = 512 * acc - 8 * sum(W): exact integers below 2^24
-          const float raw_re = fmaf(__uint_as_float(r[i]), 512.0f, -br[i]);
-          const float raw_im = fmaf(__uint_as_float(r[8 + i]), 512.0f, -bi[i]);
-          // clamp(lrint(G * float(raw)), -7, 7) + 8: one IEEE multiply, clamp to +-7.25
-          // (same result after rounding), round half to even by adding kMagic
-          const float yre = fminf(fmaxf(__fmul_rn(gv[i], raw_re), -7.25f), 7.25f);
-          const float yim = fminf(fmaxf(__fmul_rn(gv[i], raw_im), -7.25f), 7.25f);
+          // clamp(lrint(G * raw), -7, 7) + 8 with acc = raw / 512 exactly: one IEEE
+          // multiply, clamp to +-7.25 (same result after rounding), round half to
+          // even by adding kMagic
+          const float yre = fminf(fmaxf(__fmul_rn(gv[i], __uint_as_float(r[i])), -7.25f), 7.25f);
+          const float yim = fminf(fmaxf(__fmul_rn(gv[i], __uint_as_float(r[8 + i])), -7.25f), 7.25f);
           qre[i] = __float_as_uint(__fadd_rn(yre, kMagic));  // low byte = Jre + 8
           qim[i] = __float_as_uint(__fadd_rn(yim, kMagic));  // low byte = Jim + 8
         }
@@ -473,16 +534,9 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
           w[h2] = prmt(x1, __shfl_xor_sync(0xffffffffu, x1, 4), sel2);  // beam 4*h2 + j4, times t..t+3
         }
         if (t_ok) {
-#pragma unroll
-          for (int h2 = 0; h2 < 2; ++h2) {
-            const int b = b0 + 8 * c + 4 * h2 + static_cast<int>(j4);
-            if (b < P.B) {
-              // J[b][f][p][t..t+3] (Jlinear, arraysizes.hxx:92)
-              uint32_t *dst = reinterpret_cast<uint32_t *>(
-                  P.J + ((static_cast<int64_t>(b) * P.F + f) * 2 + pol) * P.jpitch + t);
-              __stcs(dst, w[h2]);
-            }
-          }
+          uint8_t *dst = jrow + static_cast<int64_t>(8 * c) * bstride;
+          if (8 * c < blim) __stcs(reinterpret_cast<uint32_t *>(dst), w[0]);
+          if (8 * c + 4 < blim) __stcs(reinterpret_cast<uint32_t *>(dst + 4 * bstride), w[1]);
         }
       };
 
@@ -526,7 +580,7 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
 //   n = 16*(b/8) + 8*cj + b%8      (cj: 0 = real output, 1 = imaginary output)
 //   k = 8*(d/4)  + 4*c  + d%4      (c:  0 = real input,  1 = imaginary input)
 // W = Ar, -Ai for the real output and Ai, Ar for the imaginary output.
-__global__ void bf_prep_weights(const uint8_t *__restrict__ A, uint8_t *__restrict__ W, float *__restrict__ bias,
+__global__ void bf_prep_weights(const uint8_t *__restrict__ A, uint8_t *__restrict__ W, uint8_t *__restrict__ dig,
                                 int B, int D, int nw, int nw_pad) {
   // E4M3 codes of the integers 0..8
   const uint8_t e4m3_pos[9] = {0x00, 0x38, 0x40, 0x44, 0x48, 0x4A, 0x4C, 0x4E, 0x50};
@@ -560,7 +614,25 @@ __global__ void bf_prep_weights(const uint8_t *__restrict__ A, uint8_t *__restri
   if (threadIdx.x == 0) {
     int s = 0;
     for (int i = 0; i < static_cast<int>(blockDim.x / 32); ++i) s += red[i];
-    bias[static_cast<int64_t>(f) * nw_pad + n] = 8.0f * static_cast<float>(s);
+    // s = sum_k W[n][k], |s| <= 16 D <= 2^15, in balanced base-16 digits
+    // d0..d3 in [-8, 7] and d4 in {-1, 0, 1}; the digit row holds the E4M3
+    // codes of d0, d1, d2, d3, 4 d4 (see kDigitScale)
+    uint32_t w0 = 0, w1 = 0;
+    int rest = s;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int r = rest & 15;
+      const int dj = r >= 8 ? r - 16 : r;
+      rest = (rest - dj) >> 4;
+      const int av = dj < 0 ? -dj : dj;
+      w0 |= static_cast<uint32_t>(e4m3_pos[av] | (dj < 0 ? 0x80 : 0x00)) << (8 * j);
+    }
+    w1 = rest == 0 ? 0u : (rest > 0 ? 0x48u : 0xC8u);  // 4 * d4: +-4 or 0
+    uint32_t *row = reinterpret_cast<uint32_t *>(dig + (static_cast<int64_t>(f) * nw_pad + n) * kDigitRow);
+    row[0] = w0;
+    row[1] = w1;
+#pragma unroll
+    for (int j = 2; j < kDigitRow / 4; ++j) row[j] = 0u;
   }
 }
 
@@ -628,14 +700,15 @@ bool tc_supported(const bf_dims &d) {
   if (d.ndishes <= 0 || d.ndishes % 8 != 0) return false;  // TMA row strides: 2*D multiple of 16 bytes
   if (d.ntimes <= 0 || d.ntimes % 16 != 0) return false;   // TMA store row strides: T multiple of 16 bytes
   if (d.nbeams <= 0 || d.nfrequencies <= 0) return false;
-  if (d.ntimes > (1ll << 31) || d.nfrequencies > (1 << 20) || d.nbeams > (1 << 16) || d.ndishes > (1 << 16))
+  // ndishes <= 2048 keeps |sum_k W[n][k]| <= 2^15, the range of the offset-correction digits
+  if (d.ntimes > (1ll << 31) || d.nfrequencies > (1 << 20) || d.nbeams > (1 << 16) || d.ndishes > 2048)
     return false;
   return true;
 }
 
 cudaError_t launch_prep_weights(const TcWeights &w, const uint8_t *A, cudaStream_t s) {
   const dim3 grid(static_cast<unsigned>(w.nw_pad), static_cast<unsigned>(w.F));
-  bf_prep_weights<<<grid, 256, 0, s>>>(A, w.W, w.bias, static_cast<int>(w.B), static_cast<int>(w.D), w.nw,
+  bf_prep_weights<<<grid, 256, 0, s>>>(A, w.W, w.dig, static_cast<int>(w.B), static_cast<int>(w.D), w.nw,
                                        w.nw_pad);
   return cudaGetLastError();
 }
@@ -657,7 +730,6 @@ static cudaError_t make_problem(TcProblem &P, const TcWeights &w, int64_t T, uin
   P.ntt = static_cast<int>((T + kTT - 1) / kTT);
   P.nw_pad = w.nw_pad;
   P.G = w.G;
-  P.bias = w.bias;
   {  // E[t][f][d*p] bytes: dims {2D, F, T}
     const cuuint64_t dims[3] = {static_cast<cuuint64_t>(2 * D), static_cast<cuuint64_t>(F),
                                 static_cast<cuuint64_t>(T)};
@@ -671,6 +743,13 @@ static cudaError_t make_problem(TcProblem &P, const TcWeights &w, int64_t T, uin
     const cuuint64_t str[2] = {static_cast<cuuint64_t>(2 * D), static_cast<cuuint64_t>(2 * D * w.nw)};
     const cuuint32_t box[3] = {static_cast<cuuint32_t>(kKC), static_cast<cuuint32_t>(2 * w.nb_pass), 1};
     if (!make_map(&P.tm_w, w.W, 3, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B)) return cudaErrorInvalidValue;
+  }
+  {  // digit rows dig[f][n][32] bytes: dims {32, nw_pad, F}
+    const cuuint64_t dims[3] = {static_cast<cuuint64_t>(kDigitRow), static_cast<cuuint64_t>(w.nw_pad),
+                                static_cast<cuuint64_t>(F)};
+    const cuuint64_t str[2] = {static_cast<cuuint64_t>(kDigitRow), static_cast<cuuint64_t>(kDigitRow) * w.nw_pad};
+    const cuuint32_t box[3] = {static_cast<cuuint32_t>(kDigitRow), static_cast<cuuint32_t>(2 * w.nb_pass), 1};
+    if (!make_map(&P.tm_d, w.dig, 3, dims, str, box, CU_TENSOR_MAP_SWIZZLE_32B)) return cudaErrorInvalidValue;
   }
   return cudaSuccess;
 }

@@ -159,7 +159,7 @@ typedef struct bf_problem {
  * order x shared-memory ring plan), keeps the fastest and captures it in a
  * CUDA graph.  The buffers must stay allocated while the batch exists; their
  * contents may change between runs.  Each problem needs the tensor-core shape
- * rules (ntimes % 16 == 0, ndishes % 8 == 0, 16-byte aligned E and J). */
+ * rules (ntimes % 16 == 0, ndishes % 8 == 0, ndishes <= 2048, 16-byte aligned E and J). */
 BF_API int bf_batch_create(bf_batch **out, const bf_problem *problems, int nproblems, bf_stream_t stream);
 
 /* Runs every problem of the batch once (graph replay); asynchronous on `stream`. */
@@ -241,14 +241,14 @@ BF_API int bf_server_destroy(bf_server *server);
  * memory -- e.g. a real-time pipeline that sizes all device memory once at
  * start-up and must not allocate mid-stream, or a host framework that owns
  * the memory pool: the tensor-core pass of bf_form_beams_ex(..., BF_PTR_DEVICE,
- * ...) with its scratch (prepared weight operand, row sums, error word) in one
+ * ...) with its scratch (prepared weight operand, row-sum digits, error word) in one
  * fixed 4 MiB device array that every GPU loading the library holds until the
  * process exits.  It calls no cudaMalloc, cudaFree or other allocating routine.
  *
  * E, A, G and J are device pointers.  Limits: the tensor-core shape rules
  * (npolarizations == 2, ndishes % 8 == 0, ntimes % 16 == 0, E and J 16-byte
- * aligned; else BF_ERR_UNSUPPORTED) and
- *   256 + roundup256(4 * F * npass * 2 * nb) + F * 2 * roundup(B, 8) * 2 * D <= 4 MiB
+ * aligned, ndishes <= 2048; else BF_ERR_UNSUPPORTED) and
+ *   256 + roundup256(32 * F * npass * 2 * nb) + F * 2 * roundup(B, 8) * 2 * D <= 4 MiB
  * (npass = ceil(roundup(B, 8) / 96), nb = roundup(ceil(roundup(B, 8) / npass), 8); else
  * BF_ERR_TOO_LARGE) -- e.g. f=16, b=96, d=512 fits, f=84 does not.
  * Synchronous: returns once the pass on `stream` has finished, with its status.
