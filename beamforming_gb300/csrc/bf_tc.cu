@@ -14,7 +14,8 @@
 // subnormal and the first normal binade share the step 2^-9).  So the raw
 // ucomplex4 nibbles (value x stored as u = x + 8) become tensor-core operands
 // with one AND per 4 values.  The offset goes into the accumulator's start
-// value, which the epilogue writes before handing the accumulator over:
+// value, set by one extra MMA that opens every tile (digit rows of the row
+// sums times a constant tile, see kDigitScaleLo):
 //
 //   acc[n] = -8 * sum_k W[n][k] / 512 + sum_k u_k W[n][k] / 512
 //          = sum_k (u_k - 8) W[n][k] / 512 = raw / 512
@@ -26,16 +27,17 @@
 // IEEE multiply by 512 G (exactly G * raw) and a round-half-even conversion.
 //
 // Warp roles (one CTA per SM, persistent over tiles; warp numbers for the
-// default layout of 8 epilogue warps and 2 unpack groups, 608 threads):
-//   warps 0-7    epilogue: TMEM accumulator -> registers -> requantise -> 4x4 byte
-//                transpose across lanes -> 32-bit stores of 4 consecutive times of
-//                one beam; then the start values of the accumulator's next tile
+// default layout of 8 epilogue warps and 1 unpack group, 480 threads):
+//   warps 0-7    epilogue: TMEM accumulator -> registers -> requantise (multiply,
+//                clamp, convert, saturating nibble pack) -> 4x4 byte transpose
+//                across lanes -> 32-bit stores of 4 consecutive times of one beam
 //   warp  8      E producer: TMA of raw E boxes into a deep ring released by the unpack
 //   warp  9      TMEM allocator and single-thread MMA issuer (A operand from TMEM)
-//   warp  10     W producer: TMA of the W slice of each K stage, released by the MMA
-//   warps 11-18  unpack, groups of four taking K stages in turn: raw E bytes ->
-//                de-interleaved E4M3 operand rows written straight into tensor memory
-//                (tcgen05.st); no shared-memory operand
+//   warp  10     W producer: TMA of each tile's digit rows and of the W slice of
+//                each K stage, released by the MMA
+//   warps 11-14  unpack (groups of four take K stages in turn): raw E bytes ->
+//                de-interleaved E4M3 operand rows written straight into tensor
+//                memory (tcgen05.st); no shared-memory operand
 //
 // GEMM row r of a tile (TMEM lane r) is (t, p) = (r / 2, r % 2) for the 64 times
 // of the tile.  TMEM columns: accumulators at [0, N) and [256, 256 + N), unpacked
@@ -167,6 +169,14 @@ struct Ring {
 __device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel) {
   uint32_t r;
   asm("prmt.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(sel));
+  return r;
+}
+
+// (c << 8) | (sat4(re) << 4) | sat4(im): two integers saturated to [-8, 7] and
+// packed as the nibbles of one byte below the bytes of c.
+__device__ __forceinline__ uint32_t pack_s4x2(int re, int im, uint32_t c) {
+  uint32_t r;
+  asm("cvt.pack.sat.s4.s32.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(re), "r"(im), "r"(c));
   return r;
 }
 
@@ -399,7 +409,9 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
           break;
         }
         const uint32_t col = tmem_base + lane_addr + stage_col(s, ncols, per_half);
-        bool slot_ok = true;
+        // the whole stage goes to registers first, so that only the tensor-memory
+        // stores wait for the tensor core to release the stage
+        uint32_t out[kSub][32];
 #pragma unroll
         for (int h = 0; h < kSub; ++h) {
           const uint8_t *raw = sR + r * kRawBytes + h * kRawBox;
@@ -411,25 +423,20 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
             e[2 * j] = prmt(w.x, w.y, sel);
             e[2 * j + 1] = prmt(w.z, w.w, sel);
           }
-          if (h == kSub - 1) mbar_arrive(raw_empty(r));  // the raw slot is in registers now
-          uint32_t out[32];
           const uint32_t msk = 0x0F0F0F0Fu;
 #pragma unroll
           for (int m = 0; m < 16; ++m) {
-            out[2 * m] = (e[m] >> 4) & msk;  // real nibbles u (E4M3 bytes = u * 2^-9)
-            out[2 * m + 1] = e[m] & msk;     // imaginary nibbles
+            out[h][2 * m] = (e[m] >> 4) & msk;  // real nibbles u (E4M3 bytes = u * 2^-9)
+            out[h][2 * m + 1] = e[m] & msk;     // imaginary nibbles
           }
-          if (h == 0) {
-            // only now wait for the tensor core to release this operand stage
-            slot_ok = __all_sync(0xffffffffu, mbar_wait(empty(s), ar.phase ^ 1u, err, kDevTimeoutEmpty));
-            if (!slot_ok) break;
-          }
-          tmem_st_32x32b_x32(col + 32 * h, out);
         }
-        if (!slot_ok) {
+        mbar_arrive(raw_empty(r));  // the raw slot is in registers now
+        if (!__all_sync(0xffffffffu, mbar_wait(empty(s), ar.phase ^ 1u, err, kDevTimeoutEmpty))) {
           ok = false;
           break;
         }
+#pragma unroll
+        for (int h = 0; h < kSub; ++h) tmem_st_32x32b_x32(col + 32 * h, out[h]);
         tmem_st_wait();
         tc_fence_before();
         mbar_arrive(a_full(s));
@@ -454,7 +461,6 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
     const uint32_t sel1 = (j4 & 1) ? 0x3715u : 0x6240u;
     const uint32_t sel2 = (j4 & 2) ? 0x3276u : 0x5410u;
     const int gstride = p.max_nb_pass;  // floats per gain entry
-    const float kMagic = 12582920.0f;  // 1.5 * 2^23 + 8: x + kMagic has rint(x) + 8 in its low mantissa bits
 
     // Gain entry of a tile's (frequency, beam pass): 512 * G[b0 + i].  The
     // accumulator ends at raw / 512 exactly, and the power-of-two scaling is
@@ -510,26 +516,23 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
         const float4 ga = *reinterpret_cast<const float4 *>(gcur + 8 * c);
         const float4 gb = *reinterpret_cast<const float4 *>(gcur + 8 * c + 4);
         const float gv[8] = {ga.x, ga.y, ga.z, ga.w, gb.x, gb.y, gb.z, gb.w};
-        uint32_t qre[8], qim[8];
+        // clamp(lrint(G * raw), -7, 7) with acc = raw / 512 exactly: one IEEE
+        // multiply, the lower clamp (to -7.25: same result after rounding), a
+        // round-half-even conversion, and the upper clamp by the saturating pack
+        int qre[8], qim[8];
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
-          // clamp(lrint(G * raw), -7, 7) + 8 with acc = raw / 512 exactly: one IEEE
-          // multiply, clamp to +-7.25 (same result after rounding), round half to
-          // even by adding kMagic
-          const float yre = fminf(fmaxf(__fmul_rn(gv[i], __uint_as_float(r[i])), -7.25f), 7.25f);
-          const float yim = fminf(fmaxf(__fmul_rn(gv[i], __uint_as_float(r[8 + i])), -7.25f), 7.25f);
-          qre[i] = __float_as_uint(__fadd_rn(yre, kMagic));  // low byte = Jre + 8
-          qim[i] = __float_as_uint(__fadd_rn(yim, kMagic));  // low byte = Jim + 8
+          qre[i] = __float2int_rn(fmaxf(__fmul_rn(gv[i], __uint_as_float(r[i])), -7.25f));
+          qim[i] = __float2int_rn(fmaxf(__fmul_rn(gv[i], __uint_as_float(r[8 + i])), -7.25f));
         }
         // ucomplex4 bytes of beams 0-3 and 4-7 for this lane's time
         uint32_t w[2];
 #pragma unroll
         for (int h2 = 0; h2 < 2; ++h2) {
-          const uint32_t rr = prmt(prmt(qre[4 * h2], qre[4 * h2 + 1], 0x0040u),
-                                   prmt(qre[4 * h2 + 2], qre[4 * h2 + 3], 0x0040u), 0x5410u);
-          const uint32_t ii = prmt(prmt(qim[4 * h2], qim[4 * h2 + 1], 0x0040u),
-                                   prmt(qim[4 * h2 + 2], qim[4 * h2 + 3], 0x0040u), 0x5410u);
-          const uint32_t x = rr * 16u + ii;  // (re nibble << 4) | im nibble, per byte
+          uint32_t x = 0;
+#pragma unroll
+          for (int j = 3; j >= 0; --j) x = pack_s4x2(qre[4 * h2 + j], qim[4 * h2 + j], x);
+          x ^= 0x88888888u;  // byte j = ucomplex4 of beam 4 * h2 + j (icomplex4.hxx:33)
           const uint32_t x1 = prmt(x, __shfl_xor_sync(0xffffffffu, x, 2), sel1);
           w[h2] = prmt(x1, __shfl_xor_sync(0xffffffffu, x1, 4), sel2);  // beam 4*h2 + j4, times t..t+3
         }
