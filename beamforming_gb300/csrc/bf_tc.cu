@@ -337,6 +337,7 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
     if (lane == 0) {
       Ring ar(S), wr(SW), dr(kDigSlots);
       const uint64_t a_const = smem_desc_sw32(smem_u32(sA));
+      const uint64_t w_desc0 = smem_desc_sw128(smem_u32(sW));
       uint32_t local = 0;
       bool ok = true;
       for (int tile = blockIdx.x; ok && tile < p.ntiles; tile += gridDim.x, ++local) {
@@ -358,22 +359,21 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
         for (int ks = 0; ks < p.nk; ++ks, ar.advance(), wr.advance()) {
           const int s = static_cast<int>(ar.idx);
           const int sw = static_cast<int>(wr.idx);
-          if (!mbar_wait(a_full(s), ar.phase, err, kDevTimeoutUnpacked) ||
-              !mbar_wait(w_full(sw), wr.phase, err, kDevTimeoutFull)) {
+          // the unpack arrives on a_full only once this stage's W slot has landed too
+          if (!mbar_wait(a_full(s), ar.phase, err, kDevTimeoutUnpacked)) {
             ok = false;
             break;
           }
           tc_fence_after();
           const uint32_t a_tmem = tmem_base + stage_col(s, ncols, per_half);
-          const uint64_t b_desc = smem_desc_sw128(smem_u32(sW + sw * sp.wbytes));
+          const uint64_t b_desc = w_desc0 + static_cast<uint64_t>((sw * sp.wbytes) >> 4);
 #pragma unroll
           for (int kk = 0; kk < kStageK / 32; ++kk) {
             // K step kk: box kk / 4, 32 bytes into its 128-byte rows (descriptor address field is in 16 B units)
             const uint64_t off = static_cast<uint64_t>(((kk >> 2) * wbox + 32 * (kk & 3)) >> 4);
             mma_f8f6f4_ts(d_tmem, a_tmem + 8 * kk, b_desc + off, idesc, 1u);
           }
-          mma_commit(empty(s));
-          mma_commit(w_empty(sw));
+          mma_commit(empty(s));  // also frees the W slot: the unpack passes it on
         }
         if (!ok) break;
         mma_commit(accfull(ab));
@@ -394,10 +394,18 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
     const uint32_t my_tiles =
         static_cast<int>(blockIdx.x) < p.ntiles ? (p.ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0u;
     const uint32_t total = my_tiles * static_cast<uint32_t>(p.nk);
-    Ring rr(R), ar(S);
+    // W slots: the tensor core's release of an operand stage (empty) also ends
+    // its use of that stage's W slot, so the group's lead lane frees the W slot
+    // of sequence it - S when it sees the stage free for sequence it, and waits
+    // for the W slot of sequence it before its a_full arrival.  One group keeps
+    // the releases in sequence order.
+    static_assert(kUnpackGroups == 1, "W slot hand-over assumes one unpack group");
+    const bool wlead = warp == kUnpackWarp0 + 4 * group && lane == 0;
+    Ring rr(R), ar(S), wr(SW), wrel(SW);
     for (int g = 0; g < group; ++g) {
       rr.advance();
       ar.advance();
+      wr.advance();
     }
     bool ok = true;
     for (uint32_t it = group; ok && it < total; it += kUnpackGroups) {
@@ -435,6 +443,12 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
           ok = false;
           break;
         }
+        if (it >= static_cast<uint32_t>(S)) {  // sequence it - S is done with its W slot
+          if (wlead) mbar_arrive(w_empty(static_cast<int>(wrel.idx)));
+          wrel.advance();
+        }
+        if (wlead && !mbar_wait(w_full(static_cast<int>(wr.idx)), wr.phase, err, kDevTimeoutFull)) ok = false;
+        if (!__all_sync(0xffffffffu, ok)) break;
 #pragma unroll
         for (int h = 0; h < kSub; ++h) tmem_st_32x32b_x32(col + 32 * h, out[h]);
         tmem_st_wait();
@@ -445,6 +459,7 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
       for (int g = 0; g < kUnpackGroups; ++g) {
         rr.advance();
         ar.advance();
+        wr.advance();
       }
     }
   } else {
