@@ -593,50 +593,58 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
   }
 }
 
-// Builds the E4M3 operand W[f][n][k] and the per-row offset correction
-// bias[f][n] = 8 * sum_k W[f][n][k] from A[f][b][d].
+// Builds the E4M3 operand W[f][n][k] and the digit rows of the row sums
+// sum_k W[f][n][k] from A[f][b][d]; one warp per row n, four k per lane-step.
 //   n = 16*(b/8) + 8*cj + b%8      (cj: 0 = real output, 1 = imaginary output)
 //   k = 8*(d/4)  + 4*c  + d%4      (c:  0 = real input,  1 = imaginary input)
 // W = Ar, -Ai for the real output and Ai, Ar for the imaginary output.
-__global__ void bf_prep_weights(const uint8_t *__restrict__ A, uint8_t *__restrict__ W, uint8_t *__restrict__ dig,
-                                int B, int D, int nw, int nw_pad) {
+constexpr int kPrepRows = 8;  // rows per 256-thread block
+__global__ void __launch_bounds__(32 * kPrepRows) bf_prep_weights(const uint8_t *__restrict__ A,
+                                                                   uint8_t *__restrict__ W,
+                                                                   uint8_t *__restrict__ dig, int B, int D, int nw,
+                                                                   int nw_pad) {
   // E4M3 codes of the integers 0..8
   const uint8_t e4m3_pos[9] = {0x00, 0x38, 0x40, 0x44, 0x48, 0x4A, 0x4C, 0x4E, 0x50};
-  const int f = blockIdx.y;
-  const int n = blockIdx.x;
+  const int rblocks = (nw_pad + kPrepRows - 1) / kPrepRows;  // blocks per frequency
+  const int f = static_cast<int>(blockIdx.x) / rblocks;
+  const int n = (static_cast<int>(blockIdx.x) % rblocks) * kPrepRows + static_cast<int>(threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (n >= nw_pad) return;  // the whole warp
   int sum = 0;
   if (n < nw) {
     const int b = 8 * (n / 16) + (n % 8);
     const int cj = (n / 8) & 1;
-    uint8_t *wrow = W + (static_cast<int64_t>(f) * nw + n) * (2 * D);
-    for (int k = threadIdx.x; k < 2 * D; k += blockDim.x) {
-      const int d = 4 * (k / 8) + (k % 4);
-      const int c = (k / 4) & 1;
-      int v = 0;
-      if (b < B) {
-        const uint32_t a = A[(static_cast<int64_t>(f) * B + b) * D + d] ^ 0x88u;
-        const int ar = static_cast<int>(static_cast<int8_t>(a)) >> 4;
-        const int ai = static_cast<int>(static_cast<int8_t>(static_cast<uint8_t>(a << 4))) >> 4;
-        v = cj == 0 ? (c == 0 ? ar : -ai) : (c == 0 ? ai : ar);
+    // rows of 2D bytes, D % 8 == 0: 4-byte aligned words
+    uint32_t *wrow = reinterpret_cast<uint32_t *>(W + (static_cast<int64_t>(f) * nw + n) * (2 * D));
+    const uint8_t *arow = A + (static_cast<int64_t>(f) * B + b) * D;
+    for (int k4 = lane; k4 < D / 2; k4 += 32) {  // k = 4 k4 .. 4 k4 + 3: dishes d0 .. d0 + 3, input part c
+      const int c = k4 & 1;
+      const int d0 = 4 * (k4 >> 1);
+      uint32_t word = 0;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        int v = 0;
+        if (b < B) {
+          const uint32_t a = arow[d0 + j] ^ 0x88u;
+          const int ar = static_cast<int>(static_cast<int8_t>(a)) >> 4;
+          const int ai = static_cast<int>(static_cast<int8_t>(static_cast<uint8_t>(a << 4))) >> 4;
+          v = cj == 0 ? (c == 0 ? ar : -ai) : (c == 0 ? ai : ar);
+        }
+        const int av = v < 0 ? -v : v;
+        word |= static_cast<uint32_t>(e4m3_pos[av] | (v < 0 ? 0x80 : 0x00)) << (8 * j);
+        sum += v;
       }
-      const int av = v < 0 ? -v : v;
-      wrow[k] = static_cast<uint8_t>(e4m3_pos[av] | (v < 0 ? 0x80 : 0x00));
-      sum += v;
+      wrow[k4] = word;
     }
   }
-  __shared__ int red[32];
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x / 32] = sum;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int s = 0;
-    for (int i = 0; i < static_cast<int>(blockDim.x / 32); ++i) s += red[i];
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  if (lane == 0) {
     // s = sum_k W[n][k], |s| <= 16 D <= 2^15, in balanced base-16 digits
     // d0..d3 in [-8, 7] and d4 in {-1, 0, 1}; the digit row holds the E4M3
-    // codes of d0, d1, d2, d3, 4 d4 (see kDigitScale)
+    // codes of d0, d1, d2, d3, 4 d4 (see kDigitScaleLo)
     uint32_t w0 = 0, w1 = 0;
-    int rest = s;
+    int rest = sum;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int r = rest & 15;
@@ -725,9 +733,10 @@ bool tc_supported(const bf_dims &d) {
 }
 
 cudaError_t launch_prep_weights(const TcWeights &w, const uint8_t *A, cudaStream_t s) {
-  const dim3 grid(static_cast<unsigned>(w.nw_pad), static_cast<unsigned>(w.F));
-  bf_prep_weights<<<grid, 256, 0, s>>>(A, w.W, w.dig, static_cast<int>(w.B), static_cast<int>(w.D), w.nw,
-                                       w.nw_pad);
+  const int64_t blocks = static_cast<int64_t>((w.nw_pad + kPrepRows - 1) / kPrepRows) * w.F;
+  if (blocks > 0x7FFFFFFF) return cudaErrorInvalidValue;
+  bf_prep_weights<<<static_cast<unsigned>(blocks), 32 * kPrepRows, 0, s>>>(A, w.W, w.dig, static_cast<int>(w.B),
+                                                                           static_cast<int>(w.D), w.nw, w.nw_pad);
   return cudaGetLastError();
 }
 
