@@ -59,6 +59,7 @@ EXPORTED_SYMBOLS = (
     "bf_batch_info",
     "bf_batch_destroy",
     "bf_tensor_peak",
+    "bf_form_beams_layout",
     "bf_server_create",
     "bf_server_submit",
     "bf_server_update_weights",
@@ -147,6 +148,7 @@ def lib() -> ctypes.CDLL:
         L.bf_status_string.argtypes = [ctypes.c_int]
         L.bf_status_string.restype = ctypes.c_char_p
         L.bf_form_beams_ex.argtypes = [D, u8p, u8p, u8p, fp, ctypes.c_int, vp]
+        L.bf_form_beams_layout.argtypes = [D, u8p, u8p, u8p, fp, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp]
         L.bf_stream_status.argtypes = [vp]
         L.bf_set_kernel.argtypes = [ctypes.c_int]
         L.bf_set_test_stall.argtypes = [ctypes.c_int]
@@ -272,6 +274,29 @@ def form_beams_ex(dims: Dims, J, E, A, G, stream=None) -> None:
     _check(
         lib().bf_form_beams_ex(ctypes.byref(d), pj, pe, pa, pg, kj, _stream_handle(stream) if kj else None),
         "bf_form_beams_ex",
+    )
+
+
+A_LAYOUTS = {"linear": 0, "a2": 1}
+J_LAYOUTS = {"linear": 0, "j2": 1}
+
+
+def form_beams_layout(dims: Dims, J, E, A, G, a_layout: str = "linear", j_layout: str = "linear",
+                      stream=None) -> None:
+    """form_beams_ex with A given in `a_layout` ("linear": A[f][b][d]; "a2":
+    A2[f][b][c][d'], ndishes 256 or 512) and J written in `j_layout`
+    ("linear": J[b][f][p][t]; "j2": J2[b][f][t][p])."""
+    pj, kj = _ptr(J, np.uint8, dims.jsize, writable=True)
+    pe, ke = _ptr(E, np.uint8, dims.esize)
+    pa, ka = _ptr(A, np.uint8, dims.asize)
+    pg, kg = _ptr(G, np.float32, 4 * dims.gsize)
+    if len({kj, ke, ka, kg}) != 1:
+        raise ValueError("E, A, G and J must all be host arrays or all CUDA tensors")
+    d = dims.c()
+    _check(
+        lib().bf_form_beams_layout(ctypes.byref(d), pj, pe, pa, pg, A_LAYOUTS[a_layout], J_LAYOUTS[j_layout], kj,
+                                   _stream_handle(stream) if kj else None),
+        "bf_form_beams_layout",
     )
 
 

@@ -139,16 +139,16 @@ int choose_tensor(const bf_dims &d, bool *use_tc) {
 
 // All four arrays on the device; the tensor-core operand goes to W / dig.
 int run_device_bufs(const bf_dims &d, uint8_t *J, const uint8_t *E, const uint8_t *A, const float *G, DevBuf &W,
-                    DevBuf &dig, int *err, cudaStream_t s);
+                    DevBuf &dig, int *err, cudaStream_t s, int a_layout = kALinear, int j_layout = kJLinear);
 
 // All four arrays on the device.  Operand scratch comes from ctx (caller holds ctx.mu).
 int run_device(DeviceCtx &c, const bf_dims &d, uint8_t *J, const uint8_t *E, const uint8_t *A, const float *G,
-               cudaStream_t s) {
-  return run_device_bufs(d, J, E, A, G, c.W, c.dig, c.err, s);
+               cudaStream_t s, int a_layout = kALinear, int j_layout = kJLinear) {
+  return run_device_bufs(d, J, E, A, G, c.W, c.dig, c.err, s, a_layout, j_layout);
 }
 
 int run_device_bufs(const bf_dims &d, uint8_t *J, const uint8_t *E, const uint8_t *A, const float *G, DevBuf &Wb,
-                    DevBuf &digb, int *err, cudaStream_t s) {
+                    DevBuf &digb, int *err, cudaStream_t s, int a_layout, int j_layout) {
   if (jsize(d) == 0) return BF_OK;
   bool use_tc = false;
   const int st = choose_tensor(d, &use_tc);
@@ -159,7 +159,7 @@ int run_device_bufs(const bf_dims &d, uint8_t *J, const uint8_t *E, const uint8_
   }
   if (!use_tc) {
     t_last_kernel = "simt";
-    return to_status(launch_simt(d, J, E, A, G, s));
+    return to_status(launch_simt(d, J, E, A, G, s, 0, a_layout, j_layout));
   }
   TcWeights w;
   plan_weights(w, d.nfrequencies, d.nbeams, d.ndishes);
@@ -168,9 +168,9 @@ int run_device_bufs(const bf_dims &d, uint8_t *J, const uint8_t *E, const uint8_
   w.W = Wb.as<uint8_t>();
   w.dig = digb.as<uint8_t>();
   w.G = G;
-  BF_TRY(launch_prep_weights(w, A, s));
+  BF_TRY(launch_prep_weights(w, A, s, a_layout));
   t_last_kernel = "tensor";
-  return to_status(launch_tc(w, d.ntimes, J, E, err, s));
+  return to_status(launch_tc(w, d.ntimes, J, E, err, s, 0, j_layout));
 }
 
 int read_and_clear_err(DeviceCtx &c, cudaStream_t s) {
@@ -203,7 +203,7 @@ int64_t chunk_times(const bf_dims &d) {
 // A, G and the tensor-core operand are uploaded / prepared once.  Synchronous;
 // the caller holds c.mu.
 int run_host_pipelined(DeviceCtx &c, const bf_dims &d, uint8_t *J, const uint8_t *E, const uint8_t *A,
-                       const float *G, cudaStream_t caller) {
+                       const float *G, cudaStream_t caller, int a_layout, int j_layout) {
   if (!c.lanes_ready) {
     for (Lane &l : c.lanes) {
       BF_TRY(cudaStreamCreateWithFlags(&l.s, cudaStreamNonBlocking));
@@ -233,7 +233,7 @@ int run_host_pipelined(DeviceCtx &c, const bf_dims &d, uint8_t *J, const uint8_t
     w.W = c.W.as<uint8_t>();
     w.dig = c.dig.as<uint8_t>();
     w.G = c.G.as<float>();
-    BF_TRY(launch_prep_weights(w, c.A.as<uint8_t>(), l0.s));
+    BF_TRY(launch_prep_weights(w, c.A.as<uint8_t>(), l0.s, a_layout));
   }
   BF_TRY(cudaEventRecord(l0.done, l0.s));
   for (int i = 1; i < kLanes; ++i) BF_TRY(cudaStreamWaitEvent(c.lanes[i].s, l0.done, 0));
@@ -243,12 +243,13 @@ int run_host_pipelined(DeviceCtx &c, const bf_dims &d, uint8_t *J, const uint8_t
     const int64_t nt = std::min(tc, T - t0);
     BF_TRY(l.E.reserve(static_cast<size_t>(nt * per_t)));
     BF_TRY(cudaMemcpyAsync(l.E.p, E + t0 * per_t, static_cast<size_t>(nt * per_t), cudaMemcpyHostToDevice, l.s));
-    uint8_t *Jc = c.J.as<uint8_t>() + t0;
+    // the chunk's first time: byte t0 of each J row, byte t0 * P of each J2 row
+    uint8_t *Jc = c.J.as<uint8_t>() + (j_layout == kJ2 ? t0 * d.npolarizations : t0);
     if (use_tc) {
-      BF_TRY(launch_tc(w, nt, Jc, l.E.as<uint8_t>(), c.err, l.s, T));
+      BF_TRY(launch_tc(w, nt, Jc, l.E.as<uint8_t>(), c.err, l.s, T, j_layout));
     } else {
       const bf_dims dc{nt, d.nfrequencies, d.ndishes, d.npolarizations, d.nbeams};
-      BF_TRY(launch_simt(dc, Jc, l.E.as<uint8_t>(), c.A.as<uint8_t>(), c.G.as<float>(), l.s, T));
+      BF_TRY(launch_simt(dc, Jc, l.E.as<uint8_t>(), c.A.as<uint8_t>(), c.G.as<float>(), l.s, T, a_layout, j_layout));
     }
   }
   for (int i = 1; i < kLanes; ++i) {
@@ -317,7 +318,15 @@ int bf_set_test_stall(int on) {
 
 int bf_form_beams_ex(const bf_dims *dims, uint8_t *J, const uint8_t *E, const uint8_t *A, const float *G,
                      int ptr_kind, bf_stream_t stream) {
+  return bf_form_beams_layout(dims, J, E, A, G, BF_A_LINEAR, BF_J_LINEAR, ptr_kind, stream);
+}
+
+int bf_form_beams_layout(const bf_dims *dims, uint8_t *J, const uint8_t *E, const uint8_t *A, const float *G,
+                         int a_layout, int j_layout, int ptr_kind, bf_stream_t stream) {
   if (!dims_valid(dims)) return BF_ERR_INVALID_ARGUMENT;
+  if ((a_layout != BF_A_LINEAR && a_layout != BF_A_A2) || (j_layout != BF_J_LINEAR && j_layout != BF_J_J2))
+    return BF_ERR_INVALID_ARGUMENT;
+  if (a_layout == BF_A_A2 && !a2_supported(dims->ndishes)) return BF_ERR_UNSUPPORTED;
   if (ptr_kind != BF_PTR_HOST && ptr_kind != BF_PTR_DEVICE) return BF_ERR_INVALID_ARGUMENT;
   const bf_dims d = *dims;
   if (jsize(d) == 0) return BF_OK;
@@ -327,11 +336,11 @@ int bf_form_beams_ex(const bf_dims *dims, uint8_t *J, const uint8_t *E, const ui
   if (st != BF_OK) return st;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   std::lock_guard<std::mutex> lk(c->mu);
-  if (ptr_kind == BF_PTR_DEVICE) return run_device(*c, d, J, E, A, G, s);
+  if (ptr_kind == BF_PTR_DEVICE) return run_device(*c, d, J, E, A, G, s, a_layout, j_layout);
 
   // Host pointers: stage in, compute, stage out, synchronously (cuda.cu:274-314 does the same around its
-  // kernel), pipelined over frequency groups when there is more than one.
-  if (chunk_times(d) < d.ntimes) return run_host_pipelined(*c, d, J, E, A, G, s);
+  // kernel), pipelined over time chunks when there is more than one.
+  if (chunk_times(d) < d.ntimes) return run_host_pipelined(*c, d, J, E, A, G, s, a_layout, j_layout);
   BF_TRY(c->E.reserve(esize(d)));
   BF_TRY(c->A.reserve(asize(d)));
   BF_TRY(c->G.reserve(gsize(d) * sizeof(float)));
@@ -339,7 +348,8 @@ int bf_form_beams_ex(const bf_dims *dims, uint8_t *J, const uint8_t *E, const ui
   BF_TRY(cudaMemcpyAsync(c->E.p, E, esize(d), cudaMemcpyHostToDevice, s));
   BF_TRY(cudaMemcpyAsync(c->A.p, A, asize(d), cudaMemcpyHostToDevice, s));
   BF_TRY(cudaMemcpyAsync(c->G.p, G, gsize(d) * sizeof(float), cudaMemcpyHostToDevice, s));
-  st = run_device(*c, d, c->J.as<uint8_t>(), c->E.as<uint8_t>(), c->A.as<uint8_t>(), c->G.as<float>(), s);
+  st = run_device(*c, d, c->J.as<uint8_t>(), c->E.as<uint8_t>(), c->A.as<uint8_t>(), c->G.as<float>(), s, a_layout,
+                  j_layout);
   if (st != BF_OK) return st;
   BF_TRY(cudaMemcpyAsync(J, c->J.p, jsize(d), cudaMemcpyDeviceToHost, s));
   return read_and_clear_err(*c, s);

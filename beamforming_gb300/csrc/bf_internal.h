@@ -10,10 +10,50 @@
 
 namespace bf {
 
+// Array layouts besides the reference's Alinear / Jlinear (arraysizes.hxx:92,
+// 115): the lossy kernel family's A2[f][b][c][d'] (A2linear, arraysizes.hxx:125,
+// dish order d' of cuda4.cu:1468-1494, two dishes' nibbles per byte) and
+// J2[b][f][t][p] (J2linear, arraysizes.hxx:103).
+enum ALayout : int { kALinear = 0, kA2 = 1 };
+enum JLayout : int { kJLinear = 0, kJ2 = 1 };
+
+// A2 is defined for ndishes 256 and 512 (its dish permutation is a bijection there).
+inline bool a2_supported(int64_t ndishes) { return ndishes == 256 || ndishes == 512; }
+
+// Position d' of dish d in A2 (cuda4.cu:1472-1476): bits 8 | 5..0 | 7..6.
+__host__ __device__ __forceinline__ int64_t a2_dish(int64_t d) {
+  return (d & 0x100) | ((d & 0x3F) << 2) | ((d >> 6) & 3);
+}
+
+#ifdef __CUDACC__
+// Signed 4-bit value of nibble i of a ucomplex4 array: odd i the high (real)
+// nibble of byte i / 2, even i the low (imaginary) one (icomplex4.hxx:33-38).
+__device__ __forceinline__ int a2_nibble(const uint8_t *A, int64_t i) {
+  const uint32_t x = static_cast<uint32_t>(A[i >> 1]) ^ 0x88u;
+  return (i & 1) ? static_cast<int>(static_cast<int8_t>(x)) >> 4
+                 : static_cast<int>(static_cast<int8_t>(static_cast<uint8_t>(x << 4))) >> 4;
+}
+
+// Real and imaginary part of the weight of dish d, beam b, frequency f.
+__device__ __forceinline__ void load_a(const uint8_t *A, int a_layout, int64_t f, int64_t b, int64_t d, int64_t B,
+                                       int64_t D, int &re, int &im) {
+  if (a_layout == kALinear) {  // A[f][b][d] (Alinear, arraysizes.hxx:115)
+    const uint32_t a = static_cast<uint32_t>(A[(f * B + b) * D + d]) ^ 0x88u;
+    re = static_cast<int>(static_cast<int8_t>(a)) >> 4;
+    im = static_cast<int>(static_cast<int8_t>(static_cast<uint8_t>(a << 4))) >> 4;
+  } else {  // A2linear(f, b, c, d') = d' + D (c + 2 (b + B f)) nibbles (arraysizes.hxx:125)
+    const int64_t base = (f * B + b) * 2 * D + a2_dish(d);
+    re = a2_nibble(A, base);
+    im = a2_nibble(A, base + D);
+  }
+}
+#endif
+
 // Exact integer SIMT kernel (dp4a); any shape with npolarizations <= 2.  J
-// rows (b, f, p) are `jpitch` bytes apart (0: ntimes).
+// rows (b, f, p) -- (b, f) for J2 -- are `jpitch` (2 * jpitch for J2) bytes
+// apart (0: ntimes).
 cudaError_t launch_simt(const bf_dims &d, uint8_t *J, const uint8_t *E, const uint8_t *A, const float *G,
-                        cudaStream_t s, int64_t jpitch = 0);
+                        cudaStream_t s, int64_t jpitch = 0, int a_layout = kALinear, int j_layout = kJLinear);
 
 // Tensor-core path ------------------------------------------------------------
 
@@ -39,14 +79,14 @@ bool tc_supported(const bf_dims &d);
 void tc_plan_beams(int64_t B, int *nb_pass, int *npass);
 
 // Fills w.W and w.dig from device A (w's sizes and buffers already set).
-cudaError_t launch_prep_weights(const TcWeights &w, const uint8_t *A, cudaStream_t s);
+cudaError_t launch_prep_weights(const TcWeights &w, const uint8_t *A, cudaStream_t s, int a_layout = kALinear);
 
 // Beamforms T times of device E into device J with prepared weights.  `err`
 // is a device int that receives a nonzero DeviceError on an expired wait.
 // J rows (b, f, p) are `jpitch` bytes apart (0: T), so a time chunk of a longer
 // pass can be written in place: E and J point at the chunk's first time.
 cudaError_t launch_tc(const TcWeights &w, int64_t T, uint8_t *J, const uint8_t *E, int *err, cudaStream_t s,
-                      int64_t jpitch = 0);
+                      int64_t jpitch = 0, int j_layout = kJLinear);
 
 // One beamforming problem of a tensor-core launch: operand descriptors,
 // pointers, shape.  A plain launch carries one inline; a grouped launch reads
@@ -57,7 +97,8 @@ struct TcProblem {  // 128-byte aligned through its tensor maps
   CUtensorMap tm_d;  // digits[f][n][32] bytes: dims {32, nw_pad, F}, box {32, 2*nb_pass, 1}, 32B swizzle
   uint8_t *J;
   const float *G;
-  int64_t jpitch;    // bytes between consecutive (b, f, p) rows of J
+  int64_t jpitch;    // bytes between consecutive (b, f, p) rows of J (J2: (b, f) rows are 2 * jpitch apart)
+  int jlayout;       // JLayout
   int T, F, B;
   int nb_pass;       // beams per pass
   int npass;
@@ -74,7 +115,7 @@ struct TcRingPlan {
 
 // Fills a problem record (tile_begin left 0) for T times of E with weights w.
 cudaError_t tc_make_problem(TcProblem &P, const TcWeights &w, int64_t T, uint8_t *J, const uint8_t *E,
-                            int64_t jpitch);
+                            int64_t jpitch, int j_layout = kJLinear);
 // Tiles of a problem, and K stages per tile for D dishes.
 int64_t tc_problem_tiles(const TcProblem &P);
 int tc_stages_per_tile(int64_t D);

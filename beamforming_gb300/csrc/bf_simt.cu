@@ -34,7 +34,8 @@ __device__ __forceinline__ int requant(float g, int raw) {
 __global__ void __launch_bounds__(kThreads) bf_form_beams_simt(uint8_t *__restrict__ J, const uint8_t *__restrict__ E,
                                                                const uint8_t *__restrict__ A,
                                                                const float *__restrict__ G, int64_t T, int64_t F,
-                                                               int64_t D, int64_t P, int64_t B, int64_t jpitch) {
+                                                               int64_t D, int64_t P, int64_t B, int64_t jpitch,
+                                                               int a_layout, int j_layout) {
   __shared__ int32_t s_er[2][kTT][kDQ + 1];
   __shared__ int32_t s_ei[2][kTT][kDQ + 1];
   __shared__ int32_t s_ar[kBB][kDQ];
@@ -78,7 +79,7 @@ __global__ void __launch_bounds__(kThreads) bf_form_beams_simt(uint8_t *__restri
       s_er[pp][tt][dq] = static_cast<int32_t>(pack4(re[0], re[1], re[2], re[3]));
       s_ei[pp][tt][dq] = static_cast<int32_t>(pack4(im[0], im[1], im[2], im[3]));
     }
-    // A[f][b][d] (Alinear, arraysizes.hxx:115).
+    // A[f][b][d] (Alinear, arraysizes.hxx:115) or A2 (arraysizes.hxx:125).
     for (int idx = tid; idx < kBB * kDQ; idx += kThreads) {
       const int bl = idx / kDQ, dq = idx % kDQ;
       const int64_t b = b0 + bl;
@@ -87,11 +88,7 @@ __global__ void __launch_bounds__(kThreads) bf_form_beams_simt(uint8_t *__restri
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
           const int64_t d = d0 + 4 * dq + i;
-          if (d < D) {
-            const uint32_t a = A[(f * B + b) * D + d];
-            re[i] = dec_re(a);
-            im[i] = dec_im(a);
-          }
+          if (d < D) load_a(A, a_layout, f, b, d, B, D, re[i], im[i]);
         }
       }
       s_ar[bl][dq] = static_cast<int32_t>(pack4(re[0], re[1], re[2], re[3]));
@@ -127,10 +124,10 @@ __global__ void __launch_bounds__(kThreads) bf_form_beams_simt(uint8_t *__restri
         const float g = G[f * B + b];  // Glinear, arraysizes.hxx:136
         const int jre = requant(g, acc_re[k]);
         const int jim = requant(g, acc_im[k]);
-        // ucomplex4(Jre, Jim) at Jlinear(b,f,p,t) (cpu.cxx:40-41, icomplex4.hxx:33)
-        J[((b * F + f) * P + p) * jpitch + t] =
-            static_cast<uint8_t>((((static_cast<uint32_t>(jre) & 15u) << 4) | (static_cast<uint32_t>(jim) & 15u)) ^
-                                 0x88u);
+        // ucomplex4(Jre, Jim) at Jlinear(b,f,p,t) (cpu.cxx:40-41, icomplex4.hxx:33) or J2linear(b,f,t,p)
+        const int64_t at = j_layout == kJ2 ? ((b * F + f) * jpitch + t) * P + p : ((b * F + f) * P + p) * jpitch + t;
+        J[at] = static_cast<uint8_t>((((static_cast<uint32_t>(jre) & 15u) << 4) | (static_cast<uint32_t>(jim) & 15u)) ^
+                                     0x88u);
       }
     }
   }
@@ -139,7 +136,7 @@ __global__ void __launch_bounds__(kThreads) bf_form_beams_simt(uint8_t *__restri
 }  // namespace
 
 cudaError_t launch_simt(const bf_dims &d, uint8_t *J, const uint8_t *E, const uint8_t *A, const float *G,
-                        cudaStream_t s, int64_t jpitch) {
+                        cudaStream_t s, int64_t jpitch, int a_layout, int j_layout) {
   if (jpitch <= 0) jpitch = d.ntimes;
   if (d.npolarizations < 1 || d.npolarizations > 2) return cudaErrorInvalidValue;
   const int64_t gx = (d.ntimes + kTT - 1) / kTT;
@@ -147,7 +144,7 @@ cudaError_t launch_simt(const bf_dims &d, uint8_t *J, const uint8_t *E, const ui
   if (gx > 0x7FFFFFFF || d.nfrequencies > 65535 || gz > 65535) return cudaErrorInvalidConfiguration;
   const dim3 grid(static_cast<unsigned>(gx), static_cast<unsigned>(d.nfrequencies), static_cast<unsigned>(gz));
   bf_form_beams_simt<<<grid, kThreads, 0, s>>>(J, E, A, G, d.ntimes, d.nfrequencies, d.ndishes, d.npolarizations,
-                                               d.nbeams, jpitch);
+                                               d.nbeams, jpitch, a_layout, j_layout);
   return cudaGetLastError();
 }
 

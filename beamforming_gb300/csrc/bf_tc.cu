@@ -470,11 +470,6 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
     const int part = warp >> 2;
     const uint32_t pol = lane & 1u;
     const uint32_t lane_addr = static_cast<uint32_t>(32 * q) << 16;
-    const uint32_t j4 = (lane >> 1) & 3u;  // position among the 4 lanes of equal polarization
-    const uint32_t g4 = lane >> 3;         // group of 4 consecutive times
-    // byte-transpose selectors: 4 lanes x 4 beams -> each lane holds one beam's 4 times
-    const uint32_t sel1 = (j4 & 1) ? 0x3715u : 0x6240u;
-    const uint32_t sel2 = (j4 & 2) ? 0x3276u : 0x5410u;
     const int gstride = p.max_nb_pass;  // floats per gain entry
 
     // Gain entry of a tile's (frequency, beam pass): 512 * G[b0 + i].  The
@@ -518,13 +513,31 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
       const bool got = mbar_wait(accfull(ab), aph, err, kDevTimeoutAccFull);
       if (!named_bar_and(2, kEpiThreads, got)) break;  // all epilogue warps leave together
       tc_fence_after();
-      const int64_t t = static_cast<int64_t>(tt) * kTT + 16 * q + 4 * g4;  // first of this lane's 4 times
-      const bool t_ok = t < P.T;
       const uint32_t acc_addr = tmem_base + ab * kAccCols + lane_addr;
-      // J[b][f][p][t..t+3] (Jlinear, arraysizes.hxx:92) of beam b0 + j4; beams are bstride bytes apart
-      const int64_t bstride = static_cast<int64_t>(P.F) * 2 * P.jpitch;
-      uint8_t *const jrow =
-          P.J + ((static_cast<int64_t>(b0 + static_cast<int>(j4)) * P.F + f) * 2 + pol) * P.jpitch + t;
+      // A 4x4 byte transpose among 4 lanes turns "4 beams of one row" into "4
+      // rows of one beam" in each lane.  Jlinear (arraysizes.hxx:92): the 4 lanes
+      // of equal polarization and consecutive times (lane bits 1 and 2) exchange,
+      // and a lane stores J[b][f][p][t..t+3].  J2linear (arraysizes.hxx:103): 4
+      // consecutive rows (t, p), (t, p+1), (t+1, p), (t+1, p+1) (lane bits 0 and
+      // 1) exchange, and a lane stores those 4 bytes of J2[b][f][t][p].
+      const bool j2 = P.jlayout == kJ2;
+      const uint32_t j4 = j2 ? (lane & 3u) : ((lane >> 1) & 3u);  // place among the 4 = beam offset after
+      const int xd1 = j2 ? 1 : 2, xd2 = j2 ? 2 : 4;
+      const uint32_t sel1 = (j4 & 1) ? 0x3715u : 0x6240u;
+      const uint32_t sel2 = (j4 & 2) ? 0x3276u : 0x5410u;
+      const int64_t bj = static_cast<int64_t>(b0 + static_cast<int>(j4)) * P.F + f;  // beam row b0 + j4
+      int64_t t;      // first time of the lane's 4 bytes
+      uint8_t *jrow;  // the lane's bytes for beam b0 + j4
+      if (!j2) {
+        t = static_cast<int64_t>(tt) * kTT + 16 * q + 4 * (lane >> 3);
+        jrow = P.J + (bj * 2 + pol) * P.jpitch + t;
+      } else {
+        const int r0 = 32 * q + static_cast<int>(lane & ~3u);  // first of the 4 rows in the tile
+        t = static_cast<int64_t>(tt) * kTT + r0 / 2;
+        jrow = P.J + bj * 2 * P.jpitch + 2 * static_cast<int64_t>(tt) * kTT + r0;
+      }
+      const bool t_ok = t < P.T;
+      const int64_t bstride = static_cast<int64_t>(P.F) * 2 * P.jpitch;  // bytes between beams, both layouts
       const int blim = P.B - b0 - static_cast<int>(j4);  // beam offsets below this exist
 
       auto process = [&](int c, const uint32_t (&r)[16]) {
@@ -548,8 +561,8 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
 #pragma unroll
           for (int j = 3; j >= 0; --j) x = pack_s4x2(qre[4 * h2 + j], qim[4 * h2 + j], x);
           x ^= 0x88888888u;  // byte j = ucomplex4 of beam 4 * h2 + j (icomplex4.hxx:33)
-          const uint32_t x1 = prmt(x, __shfl_xor_sync(0xffffffffu, x, 2), sel1);
-          w[h2] = prmt(x1, __shfl_xor_sync(0xffffffffu, x1, 4), sel2);  // beam 4*h2 + j4, times t..t+3
+          const uint32_t x1 = prmt(x, __shfl_xor_sync(0xffffffffu, x, xd1), sel1);
+          w[h2] = prmt(x1, __shfl_xor_sync(0xffffffffu, x1, xd2), sel2);  // beam 4*h2 + j4, the 4 rows
         }
         if (t_ok) {
           uint8_t *dst = jrow + static_cast<int64_t>(8 * c) * bstride;
@@ -602,7 +615,7 @@ constexpr int kPrepRows = 8;  // rows per 256-thread block
 __global__ void __launch_bounds__(32 * kPrepRows) bf_prep_weights(const uint8_t *__restrict__ A,
                                                                    uint8_t *__restrict__ W,
                                                                    uint8_t *__restrict__ dig, int B, int D, int nw,
-                                                                   int nw_pad) {
+                                                                   int nw_pad, int a_layout) {
   // E4M3 codes of the integers 0..8
   const uint8_t e4m3_pos[9] = {0x00, 0x38, 0x40, 0x44, 0x48, 0x4A, 0x4C, 0x4E, 0x50};
   const int rblocks = (nw_pad + kPrepRows - 1) / kPrepRows;  // blocks per frequency
@@ -616,7 +629,6 @@ __global__ void __launch_bounds__(32 * kPrepRows) bf_prep_weights(const uint8_t 
     const int cj = (n / 8) & 1;
     // rows of 2D bytes, D % 8 == 0: 4-byte aligned words
     uint32_t *wrow = reinterpret_cast<uint32_t *>(W + (static_cast<int64_t>(f) * nw + n) * (2 * D));
-    const uint8_t *arow = A + (static_cast<int64_t>(f) * B + b) * D;
     for (int k4 = lane; k4 < D / 2; k4 += 32) {  // k = 4 k4 .. 4 k4 + 3: dishes d0 .. d0 + 3, input part c
       const int c = k4 & 1;
       const int d0 = 4 * (k4 >> 1);
@@ -625,9 +637,8 @@ __global__ void __launch_bounds__(32 * kPrepRows) bf_prep_weights(const uint8_t 
       for (int j = 0; j < 4; ++j) {
         int v = 0;
         if (b < B) {
-          const uint32_t a = arow[d0 + j] ^ 0x88u;
-          const int ar = static_cast<int>(static_cast<int8_t>(a)) >> 4;
-          const int ai = static_cast<int>(static_cast<int8_t>(static_cast<uint8_t>(a << 4))) >> 4;
+          int ar, ai;
+          load_a(A, a_layout, f, b, d0 + j, B, D, ar, ai);
           v = cj == 0 ? (c == 0 ? ar : -ai) : (c == 0 ? ai : ar);
         }
         const int av = v < 0 ? -v : v;
@@ -732,17 +743,18 @@ bool tc_supported(const bf_dims &d) {
   return true;
 }
 
-cudaError_t launch_prep_weights(const TcWeights &w, const uint8_t *A, cudaStream_t s) {
+cudaError_t launch_prep_weights(const TcWeights &w, const uint8_t *A, cudaStream_t s, int a_layout) {
   const int64_t blocks = static_cast<int64_t>((w.nw_pad + kPrepRows - 1) / kPrepRows) * w.F;
   if (blocks > 0x7FFFFFFF) return cudaErrorInvalidValue;
   bf_prep_weights<<<static_cast<unsigned>(blocks), 32 * kPrepRows, 0, s>>>(A, w.W, w.dig, static_cast<int>(w.B),
-                                                                           static_cast<int>(w.D), w.nw, w.nw_pad);
+                                                                           static_cast<int>(w.D), w.nw, w.nw_pad,
+                                                                           a_layout);
   return cudaGetLastError();
 }
 
 // Fills a problem record: shape, pointers and the two tensor maps.
 static cudaError_t make_problem(TcProblem &P, const TcWeights &w, int64_t T, uint8_t *J, const uint8_t *E,
-                                int64_t jpitch) {
+                                int64_t jpitch, int j_layout) {
   const int64_t F = w.F, D = w.D;
   if ((reinterpret_cast<uintptr_t>(E) & 15u) || (reinterpret_cast<uintptr_t>(J) & 15u)) return cudaErrorMisalignedAddress;
   std::memset(&P, 0, sizeof(P));
@@ -752,6 +764,8 @@ static cudaError_t make_problem(TcProblem &P, const TcWeights &w, int64_t T, uin
   P.J = J;
   P.jpitch = jpitch > 0 ? jpitch : T;
   if (P.jpitch < T || (P.jpitch & 3)) return cudaErrorInvalidValue;
+  if (j_layout != kJLinear && j_layout != kJ2) return cudaErrorInvalidValue;
+  P.jlayout = j_layout;
   P.nb_pass = w.nb_pass;
   P.npass = w.npass;
   P.ntt = static_cast<int>((T + kTT - 1) / kTT);
@@ -822,8 +836,8 @@ static cudaError_t launch_kernel(const TcParams &p, int smem_bytes, cudaStream_t
 }
 
 cudaError_t tc_make_problem(TcProblem &P, const TcWeights &w, int64_t T, uint8_t *J, const uint8_t *E,
-                            int64_t jpitch) {
-  return make_problem(P, w, T, J, E, jpitch);
+                            int64_t jpitch, int j_layout) {
+  return make_problem(P, w, T, J, E, jpitch, j_layout);
 }
 
 int64_t tc_problem_tiles(const TcProblem &P) { return static_cast<int64_t>(P.ntt) * P.F * P.npass; }
@@ -845,9 +859,9 @@ cudaError_t launch_tc_grouped(const TcProblem *table, int nprob, int ntiles, int
 }
 
 cudaError_t launch_tc(const TcWeights &w, int64_t T, uint8_t *J, const uint8_t *E, int *err, cudaStream_t s,
-                      int64_t jpitch) {
+                      int64_t jpitch, int j_layout) {
   TcParams p{};
-  cudaError_t e = make_problem(p.one, w, T, J, E, jpitch);
+  cudaError_t e = make_problem(p.one, w, T, J, E, jpitch, j_layout);
   if (e != cudaSuccess) return e;
   const int64_t ntiles = static_cast<int64_t>(p.one.ntt) * w.F * w.npass;
   if (ntiles > 0x7FFFFFFF) return cudaErrorInvalidValue;

@@ -171,6 +171,23 @@ BF_API int bf_batch_info(const bf_batch *batch, int *ntiles, int *order, int *ws
 
 BF_API int bf_batch_destroy(bf_batch *batch);
 
+/* Array layouts (for bf_form_beams_layout).  BF_A_LINEAR / BF_J_LINEAR are the
+ * reference's A[f][b][d] and J[b][f][p][t] (Alinear, Jlinear; arraysizes.hxx:92,
+ * 115) used everywhere else in this API.  BF_A_A2 is the lossy kernel family's
+ * A2[f][b][c][d']: per (f, b) the real parts then the imaginary parts of all
+ * dishes as 4-bit nibbles, two per byte (even d' in the low nibble), in the dish
+ * order d' = bits 8 | 5..0 | 7..6 of d (A2linear, arraysizes.hxx:125;
+ * cuda4.cu:1468-1494); defined for ndishes 256 and 512.  BF_J_J2 is
+ * J2[b][f][t][p] (J2linear, arraysizes.hxx:103). */
+typedef enum bf_a_layout { BF_A_LINEAR = 0, BF_A_A2 = 1 } bf_a_layout;
+typedef enum bf_j_layout { BF_J_LINEAR = 0, BF_J_J2 = 1 } bf_j_layout;
+
+/* bf_form_beams_ex with A read in a_layout and J written in j_layout; the
+ * values are identical (J2 holds J's bytes permuted).  BF_ERR_UNSUPPORTED for
+ * BF_A_A2 with ndishes other than 256 or 512. */
+BF_API int bf_form_beams_layout(const bf_dims *dims, uint8_t *J, const uint8_t *E, const uint8_t *A, const float *G,
+                                int a_layout, int j_layout, int ptr_kind, bf_stream_t stream);
+
 /* Measures the dense E4M3 tensor-core rate of the current device, in
  * TFLOP/s (two flops per multiply-add): every SM issues back-to-back
  * tcgen05 MMAs of the kind the beamformer uses (M=128, N=256, K=32, A operand

@@ -140,6 +140,26 @@ void bfo_raw_sum(const bfo_dims *dm, const uint8_t *E, const uint8_t *A, int64_t
   *im = sim;
 }
 
+/* A[f][b][d] -> A2[f][b][c][d'] (A2linear, arraysizes.hxx:125-133): component c
+ * of dish d as the nibble at A2linear(f, b, c, d'), two per ucomplex4 byte (even
+ * d' in the imaginary slot, odd d' in the real slot), d' the dish order of
+ * cuda4.cu:1468-1494 (bits 8 | 5..0 | 7..6 of d; a permutation for D = 256, 512). */
+void bfo_A_to_A2(const bfo_dims *dm, uint8_t *A2, const uint8_t *A) {
+  const int64_t F = dm->nfrequencies, B = dm->nbeams, D = dm->ndishes;
+  for (int64_t f = 0; f < F; ++f)
+    for (int64_t b = 0; b < B; ++b)
+      for (int64_t c = 0; c < 2; ++c)
+        for (int64_t d = 0; d < D; ++d) {
+          const int64_t dp = (d & 0x100) | ((d & 63) << 2) | ((d >> 6) & 3);
+          const int64_t i = dp + D * (c + 2 * (b + B * f));
+          const int v = c == 0 ? bfo_decode_re(A[(f * B + b) * D + d]) : bfo_decode_im(A[(f * B + b) * D + d]);
+          uint8_t *byte = &A2[i / 2];
+          const int re = (dp % 2 == 0) ? bfo_decode_re(*byte) : v;
+          const int im = (dp % 2 == 0) ? v : bfo_decode_im(*byte);
+          *byte = bfo_encode(re, im);
+        }
+}
+
 /* J[b][f][p][t] -> J2[b][f][t][p] (J2linear, arraysizes.hxx:103-112). */
 void bfo_J_to_J2(const bfo_dims *dm, uint8_t *J2, const uint8_t *J) {
   const int64_t T = dm->ntimes, F = dm->nfrequencies, P = dm->npolarizations, B = dm->nbeams;

@@ -50,6 +50,10 @@ void bfo_raw_sum(const bfo_dims *dims, const uint8_t *E, const uint8_t *A, int64
 /* J2[b][f][t][p] layout of the lossy kernel family (J2linear, arraysizes.hxx:103). */
 void bfo_J_to_J2(const bfo_dims *dims, uint8_t *J2, const uint8_t *J);
 
+/* A2[f][b][c][d'] layout of the lossy kernel family (A2linear, arraysizes.hxx:125;
+ * dish order of cuda4.cu:1468-1494); ndishes 256 or 512. */
+void bfo_A_to_A2(const bfo_dims *dims, uint8_t *A2, const uint8_t *A);
+
 /* adler32 (adler32.c:7-20). */
 uint32_t bfo_adler32(const uint8_t *data, size_t len);
 

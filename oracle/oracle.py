@@ -91,6 +91,8 @@ def lib() -> ctypes.CDLL:
         L.bfo_raw_sum.restype = None
         L.bfo_J_to_J2.argtypes = [ctypes.POINTER(_Dims), u8p, u8p]
         L.bfo_J_to_J2.restype = None
+        L.bfo_A_to_A2.argtypes = [ctypes.POINTER(_Dims), u8p, u8p]
+        L.bfo_A_to_A2.restype = None
         L.bfo_adler32.argtypes = [u8p, ctypes.c_size_t]
         L.bfo_adler32.restype = ctypes.c_uint32
         L.bfo_setup_pattern.argtypes = [ctypes.POINTER(_Dims), u8p, u8p, ctypes.POINTER(ctypes.c_float)]
@@ -135,6 +137,16 @@ def raw_sum(dims: Dims, E: np.ndarray, A: np.ndarray, b: int, f: int, p: int, t:
     d = dims.c()
     lib().bfo_raw_sum(ctypes.byref(d), _u8(E), _u8(A), b, f, p, t, ctypes.byref(re), ctypes.byref(im))
     return re.value, im.value
+
+
+def A_to_A2(dims: Dims, A: np.ndarray) -> np.ndarray:
+    """A[f][b][d] -> A2[f][b][c][d'] (A2linear, arraysizes.hxx:125; cuda4.cu:1468-1494)."""
+    if dims.ndishes not in (256, 512):
+        raise ValueError("A2 is defined for ndishes 256 and 512")
+    A2 = np.full_like(A, 0x88)
+    d = dims.c()
+    lib().bfo_A_to_A2(ctypes.byref(d), _u8(A2), _u8(A))
+    return A2
 
 
 def J_to_J2(dims: Dims, J: np.ndarray) -> np.ndarray:

@@ -66,6 +66,12 @@ def test_invalid_arguments(bflib):
     assert L.bf_form_beams_ex(ctypes.byref(d0), None, None, None, None, 0, None) == bflib.OK
     out = ctypes.c_uint32()
     assert L.bf_adler32_device(None, 0, ctypes.byref(out), None) == bflib.OK and out.value == 1
+    # layouts are checked before any device work
+    dl = bflib.Dims(16, 1, 128, 2, 8).c()
+    assert L.bf_form_beams_layout(ctypes.byref(dl), J.ctypes.data, J.ctypes.data, J.ctypes.data, J.ctypes.data, 2, 0,
+                                  0, None) == bflib.ERR_INVALID_ARGUMENT
+    assert L.bf_form_beams_layout(ctypes.byref(dl), J.ctypes.data, J.ctypes.data, J.ctypes.data, J.ctypes.data, 1, 0,
+                                  0, None) == bflib.ERR_UNSUPPORTED  # A2 needs 256 or 512 dishes
     # server entry points check their handles before touching a device
     h = ctypes.c_void_p()
     assert L.bf_server_create(ctypes.byref(h), None, None) == bflib.ERR_INVALID_ARGUMENT

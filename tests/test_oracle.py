@@ -122,3 +122,31 @@ def test_J_to_J2_layout(oracle):
             for p in range(P):
                 for t in range(T):
                     assert J2[((b * F + f) * T + t) * P + p] == J[((b * F + f) * P + p) * T + t]
+
+
+@pytest.mark.parametrize("D", [256, 512])
+def test_A_to_A2_layout(oracle, D):
+    """Every (f, b, c, d) lands in the nibble A2linear(f, b, c, d') names, d'
+    the dish order of cuda4.cu:1468-1494 (arraysizes.hxx:125)."""
+    F, B = 2, 3
+    rng = np.random.default_rng(5)
+    A = rng.integers(0, 256, F * B * D, dtype=np.uint8)
+    dims = oracle.Dims(16, F, D, 2, B)
+    A2 = oracle.A_to_A2(dims, A)
+
+    def signed4(x):
+        return x - 16 if x >= 8 else x
+
+    perm = set()
+    for f in range(F):
+        for b in range(B):
+            for d in range(D):
+                dp = (d & 0x100) | ((d & 63) << 2) | ((d >> 6) & 3)
+                perm.add(dp)
+                a = int(A[(f * B + b) * D + d]) ^ 0x88
+                for c, want in ((0, signed4(a >> 4)), (1, signed4(a & 15))):
+                    i = dp + D * (c + 2 * (b + B * f))
+                    byte = int(A2[i // 2]) ^ 0x88
+                    got = signed4(byte >> 4) if i % 2 else signed4(byte & 15)
+                    assert got == want
+    assert perm == set(range(D))  # a permutation of the dishes
