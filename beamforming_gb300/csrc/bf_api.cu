@@ -125,7 +125,7 @@ void plan_weights(TcWeights &w, int64_t F, int64_t B, int64_t D) {
 }
 
 size_t weights_bytes(const TcWeights &w) { return static_cast<size_t>(w.F) * w.nw * 2 * w.D; }
-size_t digit_bytes(const TcWeights &w) { return static_cast<size_t>(w.F) * w.nw_pad * kDigitRow; }
+
 
 int choose_tensor(const bf_dims &d, bool *use_tc) {
   const int k = g_kernel.load();
@@ -164,9 +164,9 @@ int run_device_bufs(const bf_dims &d, uint8_t *J, const uint8_t *E, const uint8_
   TcWeights w;
   plan_weights(w, d.nfrequencies, d.nbeams, d.ndishes);
   BF_TRY(Wb.reserve(weights_bytes(w)));
-  BF_TRY(digb.reserve(digit_bytes(w)));
+  BF_TRY(digb.reserve(tc_extra_bytes(w)));
   w.W = Wb.as<uint8_t>();
-  w.dig = digb.as<uint8_t>();
+  tc_set_extra(w, digb.as<uint8_t>());
   w.G = G;
   BF_TRY(launch_prep_weights(w, A, s, a_layout));
   t_last_kernel = "tensor";
@@ -229,9 +229,9 @@ int run_host_pipelined(DeviceCtx &c, const bf_dims &d, uint8_t *J, const uint8_t
   if (use_tc) {
     plan_weights(w, d.nfrequencies, d.nbeams, d.ndishes);
     BF_TRY(c.W.reserve(weights_bytes(w)));
-    BF_TRY(c.dig.reserve(digit_bytes(w)));
+    BF_TRY(c.dig.reserve(tc_extra_bytes(w)));
     w.W = c.W.as<uint8_t>();
-    w.dig = c.dig.as<uint8_t>();
+    tc_set_extra(w, c.dig.as<uint8_t>());
     w.G = c.G.as<float>();
     BF_TRY(launch_prep_weights(w, c.A.as<uint8_t>(), l0.s, a_layout));
   }
@@ -393,7 +393,9 @@ int bf_weights_create(bf_weights **out, int64_t nfrequencies, int64_t nbeams, in
   cudaError_t e = cudaMalloc(&w->A, na);
   if (e == cudaSuccess) e = cudaMalloc(&w->G, ng * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&w->tc.W, weights_bytes(w->tc));
-  if (e == cudaSuccess) e = cudaMalloc(&w->tc.dig, digit_bytes(w->tc));
+  uint8_t *extra = nullptr;
+  if (e == cudaSuccess) e = cudaMalloc(&extra, tc_extra_bytes(w->tc));
+  if (e == cudaSuccess) tc_set_extra(w->tc, extra);
   if (e != cudaSuccess) {
     bf_weights_destroy(w);
     return to_status(e);

@@ -69,8 +69,19 @@ struct TcWeights {
   int nw_pad = 0;    // digit rows per frequency: npass * 2 * nb_pass
   uint8_t *W = nullptr;      // [F][nw][2D]
   uint8_t *dig = nullptr;    // [F][nw_pad][kDigitRow]
-  const float *G = nullptr;  // [F][B] (device)
+  float *gs = nullptr;       // [F][nw_pad / 2]: 512 * G, zero past B (the epilogue's gains)
+  const float *G = nullptr;  // [F][B] (device; read by the weight preparation)
 };
+
+// The digit rows and the scaled gains share one allocation: digit rows first
+// (F * nw_pad * 32 bytes, a multiple of 32), then the gains.
+inline size_t tc_extra_bytes(const TcWeights &w) {
+  return static_cast<size_t>(w.F) * w.nw_pad * (kDigitRow + sizeof(float) / 2);
+}
+inline void tc_set_extra(TcWeights &w, uint8_t *p) {
+  w.dig = p;
+  w.gs = reinterpret_cast<float *>(p + static_cast<size_t>(w.F) * w.nw_pad * kDigitRow);
+}
 
 // True when the tensor-core kernel handles this shape.
 bool tc_supported(const bf_dims &d);
@@ -78,7 +89,7 @@ bool tc_supported(const bf_dims &d);
 // Beams per pass and number of passes for B beams.
 void tc_plan_beams(int64_t B, int *nb_pass, int *npass);
 
-// Fills w.W and w.dig from device A (w's sizes and buffers already set).
+// Fills w.W, w.dig and w.gs from device A and w.G (w's sizes and buffers already set).
 cudaError_t launch_prep_weights(const TcWeights &w, const uint8_t *A, cudaStream_t s, int a_layout = kALinear);
 
 // Beamforms T times of device E into device J with prepared weights.  `err`
@@ -96,7 +107,7 @@ struct TcProblem {  // 128-byte aligned through its tensor maps
   CUtensorMap tm_w;  // W[f][n][k] bytes: dims {2D, nw, F}, box {128, 2*nb_pass, 1}, 128B swizzle
   CUtensorMap tm_d;  // digits[f][n][32] bytes: dims {32, nw_pad, F}, box {32, 2*nb_pass, 1}, 32B swizzle
   uint8_t *J;
-  const float *G;
+  const float *gs;   // scaled gains [F][npass * nb_pass]
   int64_t jpitch;    // bytes between consecutive (b, f, p) rows of J (J2: (b, f) rows are 2 * jpitch apart)
   int jlayout;       // JLayout
   int T, F, B;

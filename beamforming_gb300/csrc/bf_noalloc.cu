@@ -12,7 +12,8 @@
 //
 //   g_noalloc_scratch   kNoAllocScratchBytes = 4 MiB, 256-byte aligned
 //     [0, 256)                    device error word (cleared every call)
-//     [256, 256 + digit bytes)    dig[f][n][32] E4M3, F * npass * 2 * nb_pass * 32
+//     [256, 256 + extra bytes)    dig[f][n][32] E4M3, F * npass * 2 * nb_pass * 32, then
+//                                 512 * G[f][b] floats, F * npass * nb_pass
 //     [.., .. + W bytes)          W[f][n][k]   E4M3,  F * 2 * roundup(B, 8) * 2 * D
 //
 // Every GPU that loads the library holds these 4 MiB until the process exits.
@@ -84,7 +85,7 @@ extern "C" int bf_form_beams_noalloc(const bf_dims *dims, uint8_t *J, const uint
   tc_plan_beams(d.nbeams, &w.nb_pass, &w.npass);
   w.nw = static_cast<int>((d.nbeams + 7) / 8 * 8 * 2);
   w.nw_pad = w.npass * 2 * w.nb_pass;
-  const size_t dig_bytes = static_cast<size_t>(w.F) * w.nw_pad * kDigitRow;
+  const size_t dig_bytes = tc_extra_bytes(w);
   const size_t w_bytes = static_cast<size_t>(w.F) * w.nw * 2 * w.D;
   if (kErrBytes + round256(dig_bytes) + w_bytes > kNoAllocScratchBytes) return BF_ERR_TOO_LARGE;
 
@@ -97,7 +98,7 @@ extern "C" int bf_form_beams_noalloc(const bf_dims *dims, uint8_t *J, const uint
   if (e != cudaSuccess) return status_of(e);
   uint8_t *scratch = static_cast<uint8_t *>(base);
   int *err = reinterpret_cast<int *>(scratch);
-  w.dig = scratch + kErrBytes;
+  tc_set_extra(w, scratch + kErrBytes);
   w.W = scratch + kErrBytes + round256(dig_bytes);
   w.G = G;
 

@@ -164,6 +164,7 @@ TcWeights channel_view(const TcWeights &w, int c0, int n) {
   v.F = n;
   v.W = w.W + static_cast<int64_t>(c0) * w.nw * 2 * w.D;
   v.dig = w.dig + static_cast<int64_t>(c0) * w.nw_pad * kDigitRow;
+  v.gs = w.gs + static_cast<int64_t>(c0) * (w.nw_pad / 2);
   v.G = w.G + static_cast<int64_t>(c0) * w.B;
   return v;
 }

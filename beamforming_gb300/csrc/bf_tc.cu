@@ -57,16 +57,21 @@ namespace {
 // Warp layout: kEpiWarps epilogue warps, the three single-thread roles, then
 // kUnpackGroups groups of four unpack warps.  A warp reaches TMEM lanes
 // 32 * (warp % 4) .. + 31 only, so every role that touches TMEM rows comes in
-// fours covering the four lane quarters.
-constexpr int kEpiWarps = 8;
-constexpr int kUnpackGroups = 1;
-constexpr int kEpiThreads = 32 * kEpiWarps;
-constexpr int kEpiParts = kEpiWarps / 4;  // column parts: each is read by four warps (one per lane quarter)
-constexpr int kEProdWarp = kEpiWarps;
-constexpr int kMmaWarp = kEpiWarps + 1;
-constexpr int kWProdWarp = kEpiWarps + 2;
-constexpr int kUnpackWarp0 = kEpiWarps + 3;
-constexpr int kThreads = 32 * (kUnpackWarp0 + 4 * kUnpackGroups);
+// fours covering the four lane quarters.  Twelve epilogue warps suit short K
+// (ndishes <= 512: the epilogue paces the tiles), eight suit long K (the
+// unpack does, and more epilogue warps take its issue slots).
+template <int kEpiWarps_>
+struct Roles {
+  static constexpr int kEpiWarps = kEpiWarps_;
+  static constexpr int kUnpackGroups = 1;
+  static constexpr int kEpiThreads = 32 * kEpiWarps;
+  static constexpr int kEpiParts = kEpiWarps / 4;  // column parts: each read by four warps (one per lane quarter)
+  static constexpr int kEProdWarp = kEpiWarps;
+  static constexpr int kMmaWarp = kEpiWarps + 1;
+  static constexpr int kWProdWarp = kEpiWarps + 2;
+  static constexpr int kUnpackWarp0 = kEpiWarps + 3;
+  static constexpr int kThreads = 32 * (kUnpackWarp0 + 4 * kUnpackGroups);
+};
 constexpr int kTT = 64;                 // times per tile
 constexpr int kBM = 128;                // GEMM rows per tile
 constexpr int kKC = 128;                // K bytes per TMA box / swizzle atom (64 dishes x re/im)
@@ -126,7 +131,7 @@ __device__ __forceinline__ const TcProblem &problem_of(const TcParams &p, int ti
 
 struct SmemPlan {
   int wbox, wbytes, dbytes;
-  int off_w, off_a, off_d, off_r, off_g, off_bar, nbar, total;
+  int off_w, off_a, off_d, off_r, off_bar, nbar, total;
 };
 
 __host__ __device__ inline SmemPlan smem_plan(int stages, int wslots, int raw, int nb_pass) {
@@ -138,9 +143,7 @@ __host__ __device__ inline SmemPlan smem_plan(int stages, int wslots, int raw, i
   s.off_a = s.off_w + wslots * s.wbytes;  // constant A tile of the offset MMA
   s.off_d = s.off_a + kConstABytes;       // digit-row slots
   s.off_r = s.off_d + kDigSlots * s.dbytes;
-  // two gain entries (this tile's and the next tile's): 512 * G [nb_pass]
-  s.off_g = s.off_r + raw * kRawBytes;
-  s.off_bar = s.off_g + 2 * nb_pass * 4;
+  s.off_bar = s.off_r + raw * kRawBytes;
   // raw_full[R], raw_empty[R], w_full[SW], w_empty[SW], a_full[S], empty[S], accfull[2], accempty[2],
   // d_full[2], d_empty[2]
   s.nbar = 2 * raw + 2 * wslots + 2 * stages + 4 + 2 * kDigSlots;
@@ -185,8 +188,12 @@ __device__ __forceinline__ uint32_t sw128_offset(uint32_t r, uint32_t j) {
   return (r >> 3) * 1024u + (r & 7u) * 128u + ((j ^ (r & 7u)) << 4);
 }
 
-template <bool kGrouped>
-__global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_constant__ TcParams p) {
+template <bool kGrouped, bool kJ2, int kEpiW>
+__global__ void __launch_bounds__(Roles<kEpiW>::kThreads, 1) bf_form_beams_tc(const __grid_constant__ TcParams p) {
+  using RL = Roles<kEpiW>;
+  constexpr int kEpiThreads = RL::kEpiThreads, kEpiParts = RL::kEpiParts, kEProdWarp = RL::kEProdWarp;
+  constexpr int kMmaWarp = RL::kMmaWarp, kWProdWarp = RL::kWProdWarp, kUnpackWarp0 = RL::kUnpackWarp0;
+  constexpr int kUnpackGroups = RL::kUnpackGroups;
   extern __shared__ uint8_t smem_dyn[];
   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_dyn) + 1023) & ~uintptr_t(1023));
   const int S = p.stages, SW = p.wslots, R = p.raw;
@@ -195,7 +202,6 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
   uint8_t *sA = smem + sp.off_a;
   uint8_t *sD = smem + sp.off_d;
   uint8_t *sR = smem + sp.off_r;
-  float *sG = reinterpret_cast<float *>(smem + sp.off_g);
   const uint32_t bar0 = smem_u32(smem + sp.off_bar);
   auto raw_full = [&](int r) { return bar0 + 8u * r; };
   auto raw_empty = [&](int r) { return bar0 + 8u * (R + r); };
@@ -395,13 +401,16 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
         static_cast<int>(blockIdx.x) < p.ntiles ? (p.ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0u;
     const uint32_t total = my_tiles * static_cast<uint32_t>(p.nk);
     // W slots: the tensor core's release of an operand stage (empty) also ends
-    // its use of that stage's W slot, so the group's lead lane frees the W slot
-    // of sequence it - S when it sees the stage free for sequence it, and waits
-    // for the W slot of sequence it before its a_full arrival.  One group keeps
-    // the releases in sequence order.
-    static_assert(kUnpackGroups == 1, "W slot hand-over assumes one unpack group");
+    // its use of that stage's W slot, so the lead lane of the group handling
+    // sequence it frees the W slot of sequence it - S when it sees the stage
+    // free, and waits for the W slot of sequence it before its a_full arrival.
+    // With SW >= S (the planner's rule) the releases of each slot come in
+    // order for any number of groups: the release of sequence j precedes the
+    // a_full arrival of j + S, and the next use of its slot, j + SW, is
+    // released only after the tensor core consumed j + SW >= j + S.
     const bool wlead = warp == kUnpackWarp0 + 4 * group && lane == 0;
-    Ring rr(R), ar(S), wr(SW), wrel(SW);
+    Ring rr(R), ar(S), wr(SW);
+    int relslot = ((group - S) % SW + SW) % SW;  // W slot of sequence it - S
     for (int g = 0; g < group; ++g) {
       rr.advance();
       ar.advance();
@@ -443,10 +452,7 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
           ok = false;
           break;
         }
-        if (it >= static_cast<uint32_t>(S)) {  // sequence it - S is done with its W slot
-          if (wlead) mbar_arrive(w_empty(static_cast<int>(wrel.idx)));
-          wrel.advance();
-        }
+        if (it >= static_cast<uint32_t>(S) && wlead) mbar_arrive(w_empty(relslot));  // sequence it - S is done
         if (wlead && !mbar_wait(w_full(static_cast<int>(wr.idx)), wr.phase, err, kDevTimeoutFull)) ok = false;
         if (!__all_sync(0xffffffffu, ok)) break;
 #pragma unroll
@@ -460,6 +466,7 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
         rr.advance();
         ar.advance();
         wr.advance();
+        relslot = relslot + 1 == SW ? 0 : relslot + 1;
       }
     }
   } else {
@@ -470,23 +477,10 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
     const int part = warp >> 2;
     const uint32_t pol = lane & 1u;
     const uint32_t lane_addr = static_cast<uint32_t>(32 * q) << 16;
-    const int gstride = p.max_nb_pass;  // floats per gain entry
 
-    // Gain entry of a tile's (frequency, beam pass): 512 * G[b0 + i].  The
-    // accumulator ends at raw / 512 exactly, and the power-of-two scaling is
-    // exact, so (512 G) * (raw / 512) rounds like G * raw (cpu.cxx:37).
-    auto gain_value = [&](int tile, int i) -> float {
-      int lt;
-      const TcProblem &Q = problem_of<kGrouped>(p, tile, lt);
-      if (i >= Q.nb_pass) return 0.0f;
-      const int pass = lt % Q.npass;
-      const int f = lt / (Q.npass * Q.ntt);
-      const int b0 = pass * Q.nb_pass;
-      return (b0 + i < Q.B) ? 512.0f * __ldg(Q.G + static_cast<int64_t>(f) * Q.B + b0 + i) : 0.0f;
-    };
-    if (static_cast<int>(blockIdx.x) < p.ntiles)
-      for (int i = threadIdx.x; i < gstride; i += kEpiThreads) sG[i] = gain_value(blockIdx.x, i);
-
+    // The warps of the epilogue share no barrier: each reads its chunks' gains
+    // straight from the scaled-gain rows gs = 512 * G (L1-resident) and waits for
+    // the accumulator on its own, so a slow warp does not hold up the others.
     uint32_t local = 0;
     for (int tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x, ++local) {
       int lt;
@@ -499,19 +493,11 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
       const uint32_t ab = local & 1u;
       const uint32_t aph = (local >> 1) & 1u;
       const int b0 = pass * P.nb_pass;
-      const float *gcur = sG + (local & 1u) * gstride;
-      float *gnext = sG + ((local + 1) & 1u) * gstride;
-      named_bar_sync(1, kEpiThreads);  // this tile's gains are written; last tile's readers are done
-      // next tile's gains: loads in flight during this tile, stored at its end
-      const int next = tile + static_cast<int>(gridDim.x);
-      float pre[2] = {0.0f, 0.0f};
-#pragma unroll
-      for (int k = 0; k < 2; ++k) {
-        const int i = static_cast<int>(threadIdx.x) + k * kEpiThreads;
-        if (next < p.ntiles && i < gstride) pre[k] = gain_value(next, i);
-      }
-      const bool got = mbar_wait(accfull(ab), aph, err, kDevTimeoutAccFull);
-      if (!named_bar_and(2, kEpiThreads, got)) break;  // all epilogue warps leave together
+      // 512 * G[f][b0 ..] (zero beyond B): the accumulator ends at raw / 512
+      // exactly and the power-of-two scaling is exact, so (512 G) * (raw / 512)
+      // rounds like G * raw (cpu.cxx:37)
+      const float *gcur = P.gs + static_cast<int64_t>(f) * P.npass * P.nb_pass + b0;
+      if (!__all_sync(0xffffffffu, mbar_wait(accfull(ab), aph, err, kDevTimeoutAccFull))) break;
       tc_fence_after();
       const uint32_t acc_addr = tmem_base + ab * kAccCols + lane_addr;
       // A 4x4 byte transpose among 4 lanes turns "4 beams of one row" into "4
@@ -520,7 +506,7 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
       // and a lane stores J[b][f][p][t..t+3].  J2linear (arraysizes.hxx:103): 4
       // consecutive rows (t, p), (t, p+1), (t+1, p), (t+1, p+1) (lane bits 0 and
       // 1) exchange, and a lane stores those 4 bytes of J2[b][f][t][p].
-      const bool j2 = P.jlayout == kJ2;
+      constexpr bool j2 = kJ2;
       const uint32_t j4 = j2 ? (lane & 3u) : ((lane >> 1) & 3u);  // place among the 4 = beam offset after
       const int xd1 = j2 ? 1 : 2, xd2 = j2 ? 2 : 4;
       const uint32_t sel1 = (j4 & 1) ? 0x3715u : 0x6240u;
@@ -541,8 +527,8 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
       const int blim = P.B - b0 - static_cast<int>(j4);  // beam offsets below this exist
 
       auto process = [&](int c, const uint32_t (&r)[16]) {
-        const float4 ga = *reinterpret_cast<const float4 *>(gcur + 8 * c);
-        const float4 gb = *reinterpret_cast<const float4 *>(gcur + 8 * c + 4);
+        const float4 ga = __ldg(reinterpret_cast<const float4 *>(gcur + 8 * c));
+        const float4 gb = __ldg(reinterpret_cast<const float4 *>(gcur + 8 * c + 4));
         const float gv[8] = {ga.x, ga.y, ga.z, ga.w, gb.x, gb.y, gb.z, gb.w};
         // clamp(lrint(G * raw), -7, 7) with acc = raw / 512 exactly: one IEEE
         // multiply, the lower clamp (to -7.25: same result after rounding), a
@@ -590,11 +576,6 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
       }
       tc_fence_before();
       mbar_arrive(accempty(ab));
-#pragma unroll
-      for (int k = 0; k < 2; ++k) {
-        const int i = static_cast<int>(threadIdx.x) + k * kEpiThreads;
-        if (next < p.ntiles && i < gstride) gnext[i] = pre[k];
-      }
     }
   }
 
@@ -614,14 +595,20 @@ __global__ void __launch_bounds__(kThreads, 1) bf_form_beams_tc(const __grid_con
 constexpr int kPrepRows = 8;  // rows per 256-thread block
 __global__ void __launch_bounds__(32 * kPrepRows) bf_prep_weights(const uint8_t *__restrict__ A,
                                                                    uint8_t *__restrict__ W,
-                                                                   uint8_t *__restrict__ dig, int B, int D, int nw,
-                                                                   int nw_pad, int a_layout) {
+                                                                   uint8_t *__restrict__ dig,
+                                                                   const float *__restrict__ G, float *__restrict__ gs,
+                                                                   int B, int D, int nw, int nw_pad, int a_layout) {
   // E4M3 codes of the integers 0..8
   const uint8_t e4m3_pos[9] = {0x00, 0x38, 0x40, 0x44, 0x48, 0x4A, 0x4C, 0x4E, 0x50};
   const int rblocks = (nw_pad + kPrepRows - 1) / kPrepRows;  // blocks per frequency
   const int f = static_cast<int>(blockIdx.x) / rblocks;
   const int n = (static_cast<int>(blockIdx.x) % rblocks) * kPrepRows + static_cast<int>(threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
+  if (static_cast<int>(blockIdx.x) % rblocks == 0) {  // the frequency's scaled gains: 512 G, zero past B
+    const int ng = nw_pad / 2;
+    for (int i = threadIdx.x; i < ng; i += blockDim.x)
+      gs[static_cast<int64_t>(f) * ng + i] = i < B ? 512.0f * G[static_cast<int64_t>(f) * B + i] : 0.0f;
+  }
   if (n >= nw_pad) return;  // the whole warp
   int sum = 0;
   if (n < nw) {
@@ -746,9 +733,8 @@ bool tc_supported(const bf_dims &d) {
 cudaError_t launch_prep_weights(const TcWeights &w, const uint8_t *A, cudaStream_t s, int a_layout) {
   const int64_t blocks = static_cast<int64_t>((w.nw_pad + kPrepRows - 1) / kPrepRows) * w.F;
   if (blocks > 0x7FFFFFFF) return cudaErrorInvalidValue;
-  bf_prep_weights<<<static_cast<unsigned>(blocks), 32 * kPrepRows, 0, s>>>(A, w.W, w.dig, static_cast<int>(w.B),
-                                                                           static_cast<int>(w.D), w.nw, w.nw_pad,
-                                                                           a_layout);
+  bf_prep_weights<<<static_cast<unsigned>(blocks), 32 * kPrepRows, 0, s>>>(
+      A, w.W, w.dig, w.G, w.gs, static_cast<int>(w.B), static_cast<int>(w.D), w.nw, w.nw_pad, a_layout);
   return cudaGetLastError();
 }
 
@@ -770,7 +756,7 @@ static cudaError_t make_problem(TcProblem &P, const TcWeights &w, int64_t T, uin
   P.npass = w.npass;
   P.ntt = static_cast<int>((T + kTT - 1) / kTT);
   P.nw_pad = w.nw_pad;
-  P.G = w.G;
+  P.gs = w.gs;
   {  // E[t][f][d*p] bytes: dims {2D, F, T}
     const cuuint64_t dims[3] = {static_cast<cuuint64_t>(2 * D), static_cast<cuuint64_t>(F),
                                 static_cast<cuuint64_t>(T)};
@@ -811,28 +797,41 @@ static cudaError_t plan_launch(TcParams &p, int max_nb_pass, const TcRingPlan &p
   while (raw < kMaxRaw && smem_plan(stages, wslots, raw + 1, max_nb_pass).total + 1024 <= kSmemLimit && want_r <= 0)
     ++raw;
   while (raw > 2 && smem_plan(stages, wslots, raw, max_nb_pass).total + 1024 > kSmemLimit) --raw;
+  // the unpack hands W slots back S stages late: at least S slots keep it moving
+  const int st = std::min(stages, wslots);
   p.max_nb_pass = max_nb_pass;
-  p.stages = stages;
+  p.stages = st;
   p.wslots = wslots;
   p.raw = raw;
   p.test_stall = g_test_stall;
-  *smem_bytes = smem_plan(stages, wslots, raw, max_nb_pass).total + 1024;
+  *smem_bytes = smem_plan(st, wslots, raw, max_nb_pass).total + 1024;
   return *smem_bytes > kSmemLimit ? cudaErrorInvalidValue : cudaSuccess;
 }
 
-template <bool kGrouped>
-static cudaError_t launch_kernel(const TcParams &p, int smem_bytes, cudaStream_t s) {
+template <bool kGrouped, bool kJ2, int kEpiW>
+static cudaError_t launch_inst(const TcParams &p, int smem_bytes, cudaStream_t s) {
   static std::atomic<bool> attr_set{false};
   if (!attr_set.load()) {
-    const cudaError_t e =
-        cudaFuncSetAttribute(bf_form_beams_tc<kGrouped>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
+    const cudaError_t e = cudaFuncSetAttribute(bf_form_beams_tc<kGrouped, kJ2, kEpiW>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
     if (e != cudaSuccess) return e;
     attr_set.store(true);
   }
   const int grid = std::min(p.ntiles, num_sms());
   if (grid <= 0) return cudaSuccess;
-  bf_form_beams_tc<kGrouped><<<grid, kThreads, smem_bytes, s>>>(p);
+  bf_form_beams_tc<kGrouped, kJ2, kEpiW><<<grid, Roles<kEpiW>::kThreads, smem_bytes, s>>>(p);
   return cudaGetLastError();
+}
+
+// Instantiation for a launch: J2 output only in plain launches; the epilogue
+// width by the K stages per tile.
+template <bool kGrouped>
+static cudaError_t launch_kernel(const TcParams &p, int smem_bytes, cudaStream_t s) {
+  const bool wide_epi = p.nk <= 4;
+  if (!kGrouped && p.one.jlayout == kJ2)
+    return wide_epi ? launch_inst<false, true, 12>(p, smem_bytes, s) : launch_inst<false, true, 8>(p, smem_bytes, s);
+  return wide_epi ? launch_inst<kGrouped, false, 12>(p, smem_bytes, s)
+                  : launch_inst<kGrouped, false, 8>(p, smem_bytes, s);
 }
 
 cudaError_t tc_make_problem(TcProblem &P, const TcWeights &w, int64_t T, uint8_t *J, const uint8_t *E,

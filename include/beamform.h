@@ -265,7 +265,7 @@ BF_API int bf_server_destroy(bf_server *server);
  * E, A, G and J are device pointers.  Limits: the tensor-core shape rules
  * (npolarizations == 2, ndishes % 8 == 0, ntimes % 16 == 0, E and J 16-byte
  * aligned, ndishes <= 2048; else BF_ERR_UNSUPPORTED) and
- *   256 + roundup256(32 * F * npass * 2 * nb) + F * 2 * roundup(B, 8) * 2 * D <= 4 MiB
+ *   256 + roundup256(68 * F * npass * nb) + F * 2 * roundup(B, 8) * 2 * D <= 4 MiB
  * (npass = ceil(roundup(B, 8) / 96), nb = roundup(ceil(roundup(B, 8) / npass), 8); else
  * BF_ERR_TOO_LARGE) -- e.g. f=16, b=96, d=512 fits, f=84 does not.
  * Synchronous: returns once the pass on `stream` has finished, with its status.
