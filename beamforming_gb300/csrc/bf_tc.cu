@@ -271,9 +271,14 @@ __global__ void __launch_bounds__(Roles<kEpiW>::kThreads, 1) bf_form_beams_tc(co
       Ring rr(R);
       uint32_t issued = 0;
       bool ok = true;
+      const TcProblem *seen = nullptr;
       for (int tile = blockIdx.x; ok && tile < p.ntiles; tile += gridDim.x) {
         int lt;
         const TcProblem &P = problem_of<kGrouped>(p, tile, lt);
+        if (kGrouped && &P != seen) {  // a table entry the host rewrites between launches
+          tensormap_acquire(&P.tm_e);
+          seen = &P;
+        }
         const int tt = (lt / P.npass) % P.ntt;
         const int f = lt / (P.npass * P.ntt);
         for (int ks = 0; ks < p.nk; ++ks, rr.advance(), ++issued) {
@@ -301,9 +306,15 @@ __global__ void __launch_bounds__(Roles<kEpiW>::kThreads, 1) bf_form_beams_tc(co
       Ring wr(SW), dr(kDigSlots);
       uint32_t it = 0, dit = 0;
       bool ok = true;
+      const TcProblem *seen = nullptr;
       for (int tile = blockIdx.x; ok && tile < p.ntiles; tile += gridDim.x) {
         int lt;
         const TcProblem &P = problem_of<kGrouped>(p, tile, lt);
+        if (kGrouped && &P != seen) {  // a table entry the host rewrites between launches
+          tensormap_acquire(&P.tm_w);
+          tensormap_acquire(&P.tm_d);
+          seen = &P;
+        }
         const int pass = lt % P.npass;
         const int f = lt / (P.npass * P.ntt);
         const int wbox = 2 * P.nb_pass * kKC;
@@ -447,7 +458,10 @@ __global__ void __launch_bounds__(Roles<kEpiW>::kThreads, 1) bf_form_beams_tc(co
             out[h][2 * m + 1] = e[m] & msk;     // imaginary nibbles
           }
         }
-        mbar_arrive(raw_empty(r));  // the raw slot is in registers now
+        // the raw slot is in registers now; the next TMA into it is an async-proxy
+        // write after these generic reads, so order them across proxies first
+        fence_proxy_async_smem();
+        mbar_arrive(raw_empty(r));
         if (!__all_sync(0xffffffffu, mbar_wait(empty(s), ar.phase ^ 1u, err, kDevTimeoutEmpty))) {
           ok = false;
           break;

@@ -90,3 +90,52 @@ def test_server_keeps_caller_weights(bflib, cuda):
 def test_tensor_peak_is_measured(bflib):
     tf = bflib.tensor_peak_tflops()
     assert 500.0 < tf < 20000.0
+
+
+def test_server_refresh_under_load(bflib, cuda):
+    """Refreshes while several grouped launches are in flight (each chunk
+    checked against a plain launch with the weights of its submission).  This
+    load once exposed a missing cross-proxy fence between the unpack's reads
+    of a raw E slot and the next TMA write into it."""
+    F, T, nver, per = 16, 4096, 9, 4
+    d = bflib.Dims(T, F, D, 2, B)
+    G = cuda.from_numpy(bflib.gains(d)).cuda()
+    As = []
+    for k in range(nver):
+        A = cuda.empty(d.asize, dtype=cuda.uint8, device="cuda")
+        bflib.fill_random_device(A, 40 + k, 1)
+        As.append(A)
+    Es = []
+    for i in range(4):
+        E = cuda.empty(d.esize, dtype=cuda.uint8, device="cuda")
+        bflib.fill_random_device(E, 60 + i, 0)
+        Es.append(E)
+    ref = bflib.ResidentWeights(F, B, D, As[0], G)
+    Jt = cuda.empty(d.jsize, dtype=cuda.uint8, device="cuda")
+    want = {}
+    for k in range(nver):
+        ref.update(As[k], G)
+        for i in range(4):
+            ref.form_beams(Jt, Es[i], T)
+            bflib.stream_status()
+            want[(k, i)] = bflib.adler32_device(Jt)
+    ref.close()
+    W = bflib.ResidentWeights(F, B, D, As[0], G)
+    cuda.cuda.synchronize()
+    bad = 0
+    for rep in range(3):
+        srv = bflib.Server(W, hbm_budget_bytes=1 << 30, max_batch=64, max_inflight=3, spin_wait=True)
+        Js = [cuda.empty(d.jsize, dtype=cuda.uint8, device="cuda") for _ in range(per * nver)]
+        subs, v = [], 0
+        for i in range(per * nver):
+            if i and i % per == 0:
+                v += 1
+                srv.update_weights(As[v], G)
+            subs.append((srv.submit(0, T, Es[i % 4], Js[i], nchannels=F), v, i % 4, i))
+        srv.drain()
+        for t, *_ in subs:
+            srv.wait(t)
+        srv.close()
+        bad += sum(bflib.adler32_device(Js[j]) != want[(v, i)] for _, v, i, j in subs)
+    W.close()
+    assert bad == 0
