@@ -27,7 +27,8 @@
 // IEEE multiply by 512 G (exactly G * raw) and a round-half-even conversion.
 //
 // Warp roles (one CTA per SM, persistent over tiles; warp numbers for the
-// default layout of 8 epilogue warps and 1 unpack group, 480 threads):
+// layout of 8 epilogue warps, 480 threads; with 12 epilogue warps, 608
+// threads, the roles after the epilogue move up by four):
 //   warps 0-7    epilogue: TMEM accumulator -> registers -> requantise (multiply,
 //                clamp, convert, saturating nibble pack) -> 4x4 byte transpose
 //                across lanes -> 32-bit stores of 4 consecutive times of one beam
