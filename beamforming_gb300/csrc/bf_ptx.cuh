@@ -79,16 +79,22 @@ __device__ __forceinline__ bool mbar_try_wait_sleep(uint32_t bar, uint32_t parit
 
 // Bounded wait for the phase with the given parity to complete.  Returns false
 // (after recording `code` in *err) when no progress was seen for
-// kWaitTimeoutNs, or when another role of the kernel already failed.
+// kWaitTimeoutNs, or when another role of the kernel already failed.  The
+// hardware ends a suspended try_wait long before the hint, so the error word
+// and the clock are read only every kPollCheck polls: reading them on every
+// poll took a fifth of the issue slots of the tensor-core kernel.
+constexpr uint32_t kPollCheck = 16;
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int *err, int code) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = globaltimer_ns();
-  for (;;) {
+  for (uint32_t i = 1;; ++i) {
     if (mbar_try_wait_sleep(bar, parity, 200000u)) return true;
-    if (*reinterpret_cast<volatile int *>(err) != 0) return false;
-    if (globaltimer_ns() - t0 > kWaitTimeoutNs) {
-      atomicCAS(err, 0, code);
-      return false;
+    if (i % kPollCheck == 0) {
+      if (*reinterpret_cast<volatile int *>(err) != 0) return false;
+      if (globaltimer_ns() - t0 > kWaitTimeoutNs) {
+        atomicCAS(err, 0, code);
+        return false;
+      }
     }
   }
 }
@@ -212,6 +218,35 @@ __device__ __forceinline__ void mma_f8f6f4_ts(uint32_t d_tmem, uint32_t a_tmem, 
       "setp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
       "r"(a_tmem), "l"(b_desc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+// The eight MMAs of one K stage (two 128-byte W boxes, b0 and b1): K step kk
+// reads TMEM columns a + 8 kk and box kk / 4 at byte 32 (kk % 4) of its rows
+// (descriptor address field in 16 B units).  One asm block and one predicate:
+// the issuing thread's instruction stream, not the tensor pipe, is the limit
+// at N = 192, so it carries nothing else.
+__device__ __forceinline__ void mma_ts_stage8(uint32_t d_tmem, uint32_t a_tmem, uint64_t b0, uint64_t b1,
+                                              uint32_t idesc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t.reg .b64 b;\n\t.reg .b32 a;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], [%1], %2, %4, p;\n\t"
+      "add.u32 a, %1, 8;\n\tadd.s64 b, %2, 2;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], [a], b, %4, p;\n\t"
+      "add.u32 a, %1, 16;\n\tadd.s64 b, %2, 4;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], [a], b, %4, p;\n\t"
+      "add.u32 a, %1, 24;\n\tadd.s64 b, %2, 6;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], [a], b, %4, p;\n\t"
+      "add.u32 a, %1, 32;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], [a], %3, %4, p;\n\t"
+      "add.u32 a, %1, 40;\n\tadd.s64 b, %3, 2;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], [a], b, %4, p;\n\t"
+      "add.u32 a, %1, 48;\n\tadd.s64 b, %3, 4;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], [a], b, %4, p;\n\t"
+      "add.u32 a, %1, 56;\n\tadd.s64 b, %3, 6;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], [a], b, %4, p;\n\t}" ::"r"(d_tmem),
+      "r"(a_tmem), "l"(b0), "l"(b1), "r"(idesc)
       : "memory");
 }
 

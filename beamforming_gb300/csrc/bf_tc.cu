@@ -78,6 +78,7 @@ constexpr int kBM = 128;                // GEMM rows per tile
 constexpr int kKC = 128;                // K bytes per TMA box / swizzle atom (64 dishes x re/im)
 constexpr int kSub = 2;                 // boxes per pipeline stage
 constexpr int kStageK = kSub * kKC;     // K bytes per stage (128 dishes x re/im): 8 MMAs
+static_assert(kSub == 2, "mma_ts_stage8 issues the eight MMAs of two W boxes");
 constexpr int kRawBox = kTT * kKC;      // raw E per box: 64 times x 64 dishes x 2 pol
 constexpr int kRawBytes = kSub * kRawBox;
 constexpr int kAccCols = 256;           // TMEM column offset of the second accumulator
@@ -385,12 +386,7 @@ __global__ void __launch_bounds__(Roles<kEpiW>::kThreads, 1) bf_form_beams_tc(co
           tc_fence_after();
           const uint32_t a_tmem = tmem_base + stage_col(s, ncols, per_half);
           const uint64_t b_desc = w_desc0 + static_cast<uint64_t>((sw * sp.wbytes) >> 4);
-#pragma unroll
-          for (int kk = 0; kk < kStageK / 32; ++kk) {
-            // K step kk: box kk / 4, 32 bytes into its 128-byte rows (descriptor address field is in 16 B units)
-            const uint64_t off = static_cast<uint64_t>(((kk >> 2) * wbox + 32 * (kk & 3)) >> 4);
-            mma_f8f6f4_ts(d_tmem, a_tmem + 8 * kk, b_desc + off, idesc, 1u);
-          }
+          mma_ts_stage8(d_tmem, a_tmem, b_desc, b_desc + static_cast<uint64_t>(wbox >> 4), idesc);
           mma_commit(empty(s));  // also frees the W slot: the unpack passes it on
         }
         if (!ok) break;
@@ -467,12 +463,13 @@ __global__ void __launch_bounds__(Roles<kEpiW>::kThreads, 1) bf_form_beams_tc(co
           ok = false;
           break;
         }
-        if (it >= static_cast<uint32_t>(S) && wlead) mbar_arrive(w_empty(relslot));  // sequence it - S is done
-        if (wlead && !mbar_wait(w_full(static_cast<int>(wr.idx)), wr.phase, err, kDevTimeoutFull)) ok = false;
-        if (!__all_sync(0xffffffffu, ok)) break;
+        // the stores first: the W-slot hand-over runs while they drain
 #pragma unroll
         for (int h = 0; h < kSub; ++h) tmem_st_32x32b_x32(col + 32 * h, out[h]);
+        if (it >= static_cast<uint32_t>(S) && wlead) mbar_arrive(w_empty(relslot));  // sequence it - S is done
+        if (wlead && !mbar_wait(w_full(static_cast<int>(wr.idx)), wr.phase, err, kDevTimeoutFull)) ok = false;
         tmem_st_wait();
+        if (!__all_sync(0xffffffffu, ok)) break;
         tc_fence_before();
         mbar_arrive(a_full(s));
       }
