@@ -131,6 +131,50 @@ __device__ __forceinline__ const TcProblem &problem_of(const TcParams &p, int ti
   }
 }
 
+// Coordinates (beam pass, 64-time block, frequency) of a CTA's tiles.  A plain
+// launch visits tiles blockIdx.x, + gridDim.x, ...: the cursor adds the grid
+// size in the same mixed radix (npass, ntt, F) instead of dividing by the
+// run-time sizes for every tile (two divisions cost ~40 instructions, and
+// every role of the CTA pays them).  A grouped launch may change problem from
+// one tile to the next, so it divides.
+struct TileCursor {
+  int pass = 0, tt = 0, f = 0;  // current tile (plain launches)
+  int dp = 0, dt = 0, df = 0;   // gridDim.x in the same radix
+  template <bool kGrouped>
+  __device__ __forceinline__ void start(const TcParams &p) {
+    if constexpr (!kGrouped) {
+      const int np = p.one.npass, nt = p.one.ntt;
+      const int b = static_cast<int>(blockIdx.x), g = static_cast<int>(gridDim.x);
+      pass = b % np;
+      tt = (b / np) % nt;
+      f = b / (np * nt);
+      dp = g % np;
+      dt = (g / np) % nt;
+      df = g / (np * nt);
+    }
+  }
+  // Coordinates of tile lt of problem P; then steps to the CTA's next tile.
+  template <bool kGrouped>
+  __device__ __forceinline__ void take(const TcProblem &P, int lt, int &pass_, int &tt_, int &f_) {
+    if constexpr (kGrouped) {
+      pass_ = lt % P.npass;
+      tt_ = (lt / P.npass) % P.ntt;
+      f_ = lt / (P.npass * P.ntt);
+    } else {
+      pass_ = pass;
+      tt_ = tt;
+      f_ = f;
+      pass += dp;
+      int c = pass >= P.npass;
+      pass -= c ? P.npass : 0;
+      tt += dt + c;
+      c = tt >= P.ntt;
+      tt -= c ? P.ntt : 0;
+      f += df + c;
+    }
+  }
+};
+
 struct SmemPlan {
   int wbox, wbytes, dbytes;
   int off_w, off_a, off_d, off_r, off_bar, nbar, total;
@@ -274,6 +318,8 @@ __global__ void __launch_bounds__(Roles<kEpiW>::kThreads, 1) bf_form_beams_tc(co
       uint32_t issued = 0;
       bool ok = true;
       const TcProblem *seen = nullptr;
+      TileCursor cur;
+      cur.start<kGrouped>(p);
       for (int tile = blockIdx.x; ok && tile < p.ntiles; tile += gridDim.x) {
         int lt;
         const TcProblem &P = problem_of<kGrouped>(p, tile, lt);
@@ -281,8 +327,9 @@ __global__ void __launch_bounds__(Roles<kEpiW>::kThreads, 1) bf_form_beams_tc(co
           tensormap_acquire(&P.tm_e);
           seen = &P;
         }
-        const int tt = (lt / P.npass) % P.ntt;
-        const int f = lt / (P.npass * P.ntt);
+        int pass, tt, f;
+        cur.take<kGrouped>(P, lt, pass, tt, f);
+        (void)pass;
         for (int ks = 0; ks < p.nk; ++ks, rr.advance(), ++issued) {
           const int r = static_cast<int>(rr.idx);
           if (!mbar_wait(raw_empty(r), rr.phase ^ 1u, err, kDevTimeoutEmpty)) {
@@ -309,6 +356,8 @@ __global__ void __launch_bounds__(Roles<kEpiW>::kThreads, 1) bf_form_beams_tc(co
       uint32_t it = 0, dit = 0;
       bool ok = true;
       const TcProblem *seen = nullptr;
+      TileCursor cur;
+      cur.start<kGrouped>(p);
       for (int tile = blockIdx.x; ok && tile < p.ntiles; tile += gridDim.x) {
         int lt;
         const TcProblem &P = problem_of<kGrouped>(p, tile, lt);
@@ -317,8 +366,9 @@ __global__ void __launch_bounds__(Roles<kEpiW>::kThreads, 1) bf_form_beams_tc(co
           tensormap_acquire(&P.tm_d);
           seen = &P;
         }
-        const int pass = lt % P.npass;
-        const int f = lt / (P.npass * P.ntt);
+        int pass, tt, f;
+        cur.take<kGrouped>(P, lt, pass, tt, f);
+        (void)tt;
         const int wbox = 2 * P.nb_pass * kKC;
         {  // the tile's digit rows, for the offset MMA
           const int ds = static_cast<int>(dr.idx);
@@ -494,12 +544,13 @@ __global__ void __launch_bounds__(Roles<kEpiW>::kThreads, 1) bf_form_beams_tc(co
     // straight from the scaled-gain rows gs = 512 * G (L1-resident) and waits for
     // the accumulator on its own, so a slow warp does not hold up the others.
     uint32_t local = 0;
+    TileCursor cur;
+    cur.start<kGrouped>(p);
     for (int tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x, ++local) {
       int lt;
       const TcProblem &P = problem_of<kGrouped>(p, tile, lt);
-      const int pass = lt % P.npass;
-      const int tt = (lt / P.npass) % P.ntt;
-      const int f = lt / (P.npass * P.ntt);
+      int pass, tt, f;
+      cur.take<kGrouped>(P, lt, pass, tt, f);
       const int nchunk = P.nb_pass / 8;
       const int c_begin = part * nchunk / kEpiParts, c_end = (part + 1) * nchunk / kEpiParts;
       const uint32_t ab = local & 1u;
@@ -537,6 +588,7 @@ __global__ void __launch_bounds__(Roles<kEpiW>::kThreads, 1) bf_form_beams_tc(co
       const bool t_ok = t < P.T;
       const int64_t bstride = static_cast<int64_t>(P.F) * 2 * P.jpitch;  // bytes between beams, both layouts
       const int blim = P.B - b0 - static_cast<int>(j4);  // beam offsets below this exist
+      uint8_t *dst = jrow + static_cast<int64_t>(8 * c_begin) * bstride;  // beam 8 c + j4 of the lane's chunk c
 
       auto process = [&](int c, const uint32_t (&r)[16]) {
         const float4 ga = __ldg(reinterpret_cast<const float4 *>(gcur + 8 * c));
@@ -563,10 +615,10 @@ __global__ void __launch_bounds__(Roles<kEpiW>::kThreads, 1) bf_form_beams_tc(co
           w[h2] = prmt(x1, __shfl_xor_sync(0xffffffffu, x1, xd2), sel2);  // beam 4*h2 + j4, the 4 rows
         }
         if (t_ok) {
-          uint8_t *dst = jrow + static_cast<int64_t>(8 * c) * bstride;
           if (8 * c < blim) __stcs(reinterpret_cast<uint32_t *>(dst), w[0]);
           if (8 * c + 4 < blim) __stcs(reinterpret_cast<uint32_t *>(dst + 4 * bstride), w[1]);
         }
+        dst += 8 * bstride;
       };
 
       // accumulator columns in chunks of 16, the next chunk's TMEM load in flight
