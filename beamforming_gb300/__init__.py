@@ -41,6 +41,7 @@ KERNELS = {"auto": 0, "tensor": 1, "simt": 2}
 # Every symbol the C header declares; the CPU tests check the library exports them.
 EXPORTED_SYMBOLS = (
     "bf_set_dims",
+    "bf_form_beams_adler",
     "form_beams",
     "bf_last_status",
     "bf_status_string",
@@ -149,6 +150,8 @@ def lib() -> ctypes.CDLL:
         L.bf_status_string.restype = ctypes.c_char_p
         L.bf_form_beams_ex.argtypes = [D, u8p, u8p, u8p, fp, ctypes.c_int, vp]
         L.bf_form_beams_layout.argtypes = [D, u8p, u8p, u8p, fp, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp]
+        L.bf_form_beams_adler.argtypes = [D, u8p, u8p, u8p, fp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                          ctypes.POINTER(ctypes.c_uint32), vp]
         L.bf_stream_status.argtypes = [vp]
         L.bf_set_kernel.argtypes = [ctypes.c_int]
         L.bf_set_test_stall.argtypes = [ctypes.c_int]
@@ -298,6 +301,27 @@ def form_beams_layout(dims: Dims, J, E, A, G, a_layout: str = "linear", j_layout
                                    _stream_handle(stream) if kj else None),
         "bf_form_beams_layout",
     )
+
+
+def form_beams_adler(dims: Dims, J, E, A, G, a_layout: str = "linear", j_layout: str = "linear",
+                     stream=None) -> int:
+    """form_beams_layout that also returns the adler32 of the whole J it wrote
+    (the checksum the reference prints after form_beams), summed inside the
+    tensor-core kernel instead of a second pass over J.  Synchronous."""
+    pj, kj = _ptr(J, np.uint8, dims.jsize, writable=True)
+    pe, ke = _ptr(E, np.uint8, dims.esize)
+    pa, ka = _ptr(A, np.uint8, dims.asize)
+    pg, kg = _ptr(G, np.float32, 4 * dims.gsize)
+    if len({kj, ke, ka, kg}) != 1:
+        raise ValueError("E, A, G and J must all be host arrays or all CUDA tensors")
+    d = dims.c()
+    out = ctypes.c_uint32(0)
+    _check(
+        lib().bf_form_beams_adler(ctypes.byref(d), pj, pe, pa, pg, A_LAYOUTS[a_layout], J_LAYOUTS[j_layout], kj,
+                                  ctypes.byref(out), _stream_handle(stream) if kj else None),
+        "bf_form_beams_adler",
+    )
+    return int(out.value)
 
 
 def stream_status(stream=None) -> None:

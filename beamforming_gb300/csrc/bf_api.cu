@@ -69,6 +69,7 @@ struct DeviceCtx {
   DevBuf E, A, G, J;        // staging for host-pointer calls
   DevBuf W, dig;            // tensor-core operand for non-resident calls
   DevBuf partials;          // adler32 partial sums
+  DevBuf adl;               // fused adler32 sums {sum d_i, sum i d_i} of the last checked call
 };
 
 constexpr int kMaxDevices = 64;
@@ -138,17 +139,23 @@ int choose_tensor(const bf_dims &d, bool *use_tc) {
 }
 
 // All four arrays on the device; the tensor-core operand goes to W / dig.
+// With `adl` set (zeroed here), a tensor-core launch also sums J for its
+// adler32 and *fused reports that it did; the SIMT kernel does not.
 int run_device_bufs(const bf_dims &d, uint8_t *J, const uint8_t *E, const uint8_t *A, const float *G, DevBuf &W,
-                    DevBuf &dig, int *err, cudaStream_t s, int a_layout = kALinear, int j_layout = kJLinear);
+                    DevBuf &dig, int *err, cudaStream_t s, int a_layout = kALinear, int j_layout = kJLinear,
+                    unsigned long long *adl = nullptr, bool *fused = nullptr);
 
 // All four arrays on the device.  Operand scratch comes from ctx (caller holds ctx.mu).
 int run_device(DeviceCtx &c, const bf_dims &d, uint8_t *J, const uint8_t *E, const uint8_t *A, const float *G,
-               cudaStream_t s, int a_layout = kALinear, int j_layout = kJLinear) {
-  return run_device_bufs(d, J, E, A, G, c.W, c.dig, c.err, s, a_layout, j_layout);
+               cudaStream_t s, int a_layout = kALinear, int j_layout = kJLinear, unsigned long long *adl = nullptr,
+               bool *fused = nullptr) {
+  return run_device_bufs(d, J, E, A, G, c.W, c.dig, c.err, s, a_layout, j_layout, adl, fused);
 }
 
 int run_device_bufs(const bf_dims &d, uint8_t *J, const uint8_t *E, const uint8_t *A, const float *G, DevBuf &Wb,
-                    DevBuf &digb, int *err, cudaStream_t s, int a_layout, int j_layout) {
+                    DevBuf &digb, int *err, cudaStream_t s, int a_layout, int j_layout, unsigned long long *adl,
+                    bool *fused) {
+  if (fused) *fused = false;
   if (jsize(d) == 0) return BF_OK;
   bool use_tc = false;
   const int st = choose_tensor(d, &use_tc);
@@ -170,7 +177,11 @@ int run_device_bufs(const bf_dims &d, uint8_t *J, const uint8_t *E, const uint8_
   w.G = G;
   BF_TRY(launch_prep_weights(w, A, s, a_layout));
   t_last_kernel = "tensor";
-  return to_status(launch_tc(w, d.ntimes, J, E, err, s, 0, j_layout));
+  if (adl) {
+    BF_TRY(cudaMemsetAsync(adl, 0, 2 * sizeof(unsigned long long), s));
+    if (fused) *fused = true;
+  }
+  return to_status(launch_tc(w, d.ntimes, J, E, err, s, 0, j_layout, adl, J));
 }
 
 int read_and_clear_err(DeviceCtx &c, cudaStream_t s) {
@@ -203,7 +214,9 @@ int64_t chunk_times(const bf_dims &d) {
 // A, G and the tensor-core operand are uploaded / prepared once.  Synchronous;
 // the caller holds c.mu.
 int run_host_pipelined(DeviceCtx &c, const bf_dims &d, uint8_t *J, const uint8_t *E, const uint8_t *A,
-                       const float *G, cudaStream_t caller, int a_layout, int j_layout) {
+                       const float *G, cudaStream_t caller, int a_layout, int j_layout,
+                       unsigned long long *adl = nullptr, bool *fused = nullptr) {
+  if (fused) *fused = false;
   if (!c.lanes_ready) {
     for (Lane &l : c.lanes) {
       BF_TRY(cudaStreamCreateWithFlags(&l.s, cudaStreamNonBlocking));
@@ -234,6 +247,10 @@ int run_host_pipelined(DeviceCtx &c, const bf_dims &d, uint8_t *J, const uint8_t
     tc_set_extra(w, c.dig.as<uint8_t>());
     w.G = c.G.as<float>();
     BF_TRY(launch_prep_weights(w, c.A.as<uint8_t>(), l0.s, a_layout));
+    if (adl) {  // every chunk's launch adds into the same sums, positions from the start of J
+      BF_TRY(cudaMemsetAsync(adl, 0, 2 * sizeof(unsigned long long), l0.s));
+      if (fused) *fused = true;
+    }
   }
   BF_TRY(cudaEventRecord(l0.done, l0.s));
   for (int i = 1; i < kLanes; ++i) BF_TRY(cudaStreamWaitEvent(c.lanes[i].s, l0.done, 0));
@@ -246,7 +263,7 @@ int run_host_pipelined(DeviceCtx &c, const bf_dims &d, uint8_t *J, const uint8_t
     // the chunk's first time: byte t0 of each J row, byte t0 * P of each J2 row
     uint8_t *Jc = c.J.as<uint8_t>() + (j_layout == kJ2 ? t0 * d.npolarizations : t0);
     if (use_tc) {
-      BF_TRY(launch_tc(w, nt, Jc, l.E.as<uint8_t>(), c.err, l.s, T, j_layout));
+      BF_TRY(launch_tc(w, nt, Jc, l.E.as<uint8_t>(), c.err, l.s, T, j_layout, adl, c.J.as<uint8_t>()));
     } else {
       const bf_dims dc{nt, d.nfrequencies, d.ndishes, d.npolarizations, d.nbeams};
       BF_TRY(launch_simt(dc, Jc, l.E.as<uint8_t>(), c.A.as<uint8_t>(), c.G.as<float>(), l.s, T, a_layout, j_layout));
@@ -274,6 +291,11 @@ int device_error_word(int **out) {
 }  // namespace bf
 
 using namespace bf;
+
+// form_beams over any pointer kind and layout; with adler_out set, also the
+// adler32 of the J it wrote (synchronous then).
+static int form_beams_impl(const bf_dims *dims, uint8_t *J, const uint8_t *E, const uint8_t *A, const float *G,
+                           int a_layout, int j_layout, int ptr_kind, bf_stream_t stream, uint32_t *adler_out);
 
 extern "C" {
 
@@ -323,24 +345,87 @@ int bf_form_beams_ex(const bf_dims *dims, uint8_t *J, const uint8_t *E, const ui
 
 int bf_form_beams_layout(const bf_dims *dims, uint8_t *J, const uint8_t *E, const uint8_t *A, const float *G,
                          int a_layout, int j_layout, int ptr_kind, bf_stream_t stream) {
+  return form_beams_impl(dims, J, E, A, G, a_layout, j_layout, ptr_kind, stream, nullptr);
+}
+
+int bf_form_beams_adler(const bf_dims *dims, uint8_t *J, const uint8_t *E, const uint8_t *A, const float *G,
+                        int a_layout, int j_layout, int ptr_kind, uint32_t *adler, bf_stream_t stream) {
+  if (!adler) return BF_ERR_INVALID_ARGUMENT;
+  return form_beams_impl(dims, J, E, A, G, a_layout, j_layout, ptr_kind, stream, adler);
+}
+
+}  // extern "C"
+
+namespace bf {
+namespace {
+
+// The adler32 of the n bytes of device J after a checked call: from the fused
+// sums when the tensor-core kernel ran, else by the separate two-kernel pass.
+// Synchronises the stream.
+int finish_adler(DeviceCtx &c, bool fused, const uint8_t *Jdev, size_t n, cudaStream_t s, uint32_t *out) {
+  if (n == 0) {
+    *out = 1u;
+    return BF_OK;
+  }
+  if (fused) {
+    unsigned long long h[2] = {0, 0};
+    BF_TRY(cudaMemcpyAsync(h, c.adl.p, sizeof(h), cudaMemcpyDeviceToHost, s));
+    BF_TRY(cudaStreamSynchronize(s));
+    *out = adler_finish(h[0], h[1], n);
+    return BF_OK;
+  }
+  BF_TRY(c.partials.reserve(static_cast<size_t>(adler_nchunks(n)) * 2 * sizeof(uint32_t)));
+  BF_TRY(launch_adler_partials(Jdev, n, c.partials.as<uint32_t>(), s));
+  BF_TRY(launch_adler_combine(c.partials.as<uint32_t>(), n, c.adler, s));
+  uint32_t h = 0;
+  BF_TRY(cudaMemcpyAsync(&h, c.adler, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  BF_TRY(cudaStreamSynchronize(s));
+  *out = h;
+  return BF_OK;
+}
+
+}  // namespace
+}  // namespace bf
+
+static int form_beams_impl(const bf_dims *dims, uint8_t *J, const uint8_t *E, const uint8_t *A, const float *G,
+                           int a_layout, int j_layout, int ptr_kind, bf_stream_t stream, uint32_t *adler_out) {
   if (!dims_valid(dims)) return BF_ERR_INVALID_ARGUMENT;
   if ((a_layout != BF_A_LINEAR && a_layout != BF_A_A2) || (j_layout != BF_J_LINEAR && j_layout != BF_J_J2))
     return BF_ERR_INVALID_ARGUMENT;
   if (a_layout == BF_A_A2 && !a2_supported(dims->ndishes)) return BF_ERR_UNSUPPORTED;
   if (ptr_kind != BF_PTR_HOST && ptr_kind != BF_PTR_DEVICE) return BF_ERR_INVALID_ARGUMENT;
   const bf_dims d = *dims;
-  if (jsize(d) == 0) return BF_OK;
+  if (jsize(d) == 0) {
+    if (adler_out) *adler_out = 1u;  // adler32 of no bytes
+    return BF_OK;
+  }
   if (!J || (esize(d) && !E) || (asize(d) && !A) || !G) return BF_ERR_INVALID_ARGUMENT;
   DeviceCtx *c = nullptr;
   int st = current_ctx(&c);
   if (st != BF_OK) return st;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   std::lock_guard<std::mutex> lk(c->mu);
-  if (ptr_kind == BF_PTR_DEVICE) return run_device(*c, d, J, E, A, G, s, a_layout, j_layout);
+  unsigned long long *adl = nullptr;
+  if (adler_out) {
+    BF_TRY(c->adl.reserve(2 * sizeof(unsigned long long)));
+    adl = c->adl.as<unsigned long long>();
+  }
+  bool fused = false;
+  if (ptr_kind == BF_PTR_DEVICE) {
+    st = run_device(*c, d, J, E, A, G, s, a_layout, j_layout, adl, &fused);
+    if (st != BF_OK || !adler_out) return st;
+    st = finish_adler(*c, fused, J, jsize(d), s, adler_out);
+    if (st != BF_OK) return st;
+    return read_and_clear_err(*c, s);
+  }
 
   // Host pointers: stage in, compute, stage out, synchronously (cuda.cu:274-314 does the same around its
   // kernel), pipelined over time chunks when there is more than one.
-  if (chunk_times(d) < d.ntimes) return run_host_pipelined(*c, d, J, E, A, G, s, a_layout, j_layout);
+  if (chunk_times(d) < d.ntimes) {
+    st = run_host_pipelined(*c, d, J, E, A, G, s, a_layout, j_layout, adl, &fused);
+    if (st != BF_OK || !adler_out) return st;
+    return finish_adler(*c, fused, c->J.as<uint8_t>(), jsize(d), s, adler_out);
+  }
   BF_TRY(c->E.reserve(esize(d)));
   BF_TRY(c->A.reserve(asize(d)));
   BF_TRY(c->G.reserve(gsize(d) * sizeof(float)));
@@ -349,11 +434,17 @@ int bf_form_beams_layout(const bf_dims *dims, uint8_t *J, const uint8_t *E, cons
   BF_TRY(cudaMemcpyAsync(c->A.p, A, asize(d), cudaMemcpyHostToDevice, s));
   BF_TRY(cudaMemcpyAsync(c->G.p, G, gsize(d) * sizeof(float), cudaMemcpyHostToDevice, s));
   st = run_device(*c, d, c->J.as<uint8_t>(), c->E.as<uint8_t>(), c->A.as<uint8_t>(), c->G.as<float>(), s, a_layout,
-                  j_layout);
+                  j_layout, adl, &fused);
   if (st != BF_OK) return st;
   BF_TRY(cudaMemcpyAsync(J, c->J.p, jsize(d), cudaMemcpyDeviceToHost, s));
+  if (adler_out) {
+    st = finish_adler(*c, fused, c->J.as<uint8_t>(), jsize(d), s, adler_out);
+    if (st != BF_OK) return st;
+  }
   return read_and_clear_err(*c, s);
 }
+
+extern "C" {
 
 void form_beams(uint8_t *J, const uint8_t *E, const uint8_t *A, const float *G) {
   bf_dims d;

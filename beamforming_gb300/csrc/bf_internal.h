@@ -96,8 +96,22 @@ cudaError_t launch_prep_weights(const TcWeights &w, const uint8_t *A, cudaStream
 // is a device int that receives a nonzero DeviceError on an expired wait.
 // J rows (b, f, p) are `jpitch` bytes apart (0: T), so a time chunk of a longer
 // pass can be written in place: E and J point at the chunk's first time.
+// With `adler` set, the epilogue also adds every J byte it stores into the
+// adler32 sums adler[0] += d_i, adler[1] += i * d_i (i = byte position from
+// jbase, taken mod 65521); the caller zeroes them first and finishes the
+// checksum with adler_finish().
 cudaError_t launch_tc(const TcWeights &w, int64_t T, uint8_t *J, const uint8_t *E, int *err, cudaStream_t s,
-                      int64_t jpitch = 0, int j_layout = kJLinear);
+                      int64_t jpitch = 0, int j_layout = kJLinear, unsigned long long *adler = nullptr,
+                      const uint8_t *jbase = nullptr);
+constexpr uint32_t kAdlerMod = 65521;
+// adler32 of n bytes from S1 = sum d_i and S2 = sum i d_i (i from 0, both taken
+// mod 65521 or not): a = 1 + S1, b = n + n S1 - S2 (adler32.c:7-20 unrolled).
+inline uint32_t adler_finish(unsigned long long s1, unsigned long long s2, unsigned long long n) {
+  const unsigned long long m = kAdlerMod;
+  const unsigned long long a = (1 + s1 % m) % m;
+  const unsigned long long b = (n % m + (n % m) * (s1 % m) % m + m - s2 % m) % m;
+  return static_cast<uint32_t>((b << 16) | a);
+}
 
 // One beamforming problem of a tensor-core launch: operand descriptors,
 // pointers, shape.  A plain launch carries one inline; a grouped launch reads
@@ -107,6 +121,8 @@ struct TcProblem {  // 128-byte aligned through its tensor maps
   CUtensorMap tm_w;  // W[f][n][k] bytes: dims {2D, nw, F}, box {128, 2*nb_pass, 1}, 128B swizzle
   CUtensorMap tm_d;  // digits[f][n][32] bytes: dims {32, nw_pad, F}, box {32, 2*nb_pass, 1}, 32B swizzle
   uint8_t *J;
+  const uint8_t *jbase;        // start of the whole J buffer: byte positions of the fused adler32
+  unsigned long long *adler;   // null, or the fused adler32 sums {sum d_i, sum i * d_i} (device)
   const float *gs;   // scaled gains [F][npass * nb_pass]
   int64_t jpitch;    // bytes between consecutive (b, f, p) rows of J (J2: (b, f) rows are 2 * jpitch apart)
   int jlayout;       // JLayout

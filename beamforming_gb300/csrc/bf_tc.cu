@@ -234,7 +234,7 @@ __device__ __forceinline__ uint32_t sw128_offset(uint32_t r, uint32_t j) {
   return (r >> 3) * 1024u + (r & 7u) * 128u + ((j ^ (r & 7u)) << 4);
 }
 
-template <bool kGrouped, bool kJ2, int kEpiW>
+template <bool kGrouped, bool kJ2, int kEpiW, bool kAdler>
 __global__ void __launch_bounds__(Roles<kEpiW>::kThreads, 1) bf_form_beams_tc(const __grid_constant__ TcParams p) {
   using RL = Roles<kEpiW>;
   constexpr int kEpiThreads = RL::kEpiThreads, kEpiParts = RL::kEpiParts, kEProdWarp = RL::kEProdWarp;
@@ -544,6 +544,9 @@ __global__ void __launch_bounds__(Roles<kEpiW>::kThreads, 1) bf_form_beams_tc(co
     // straight from the scaled-gain rows gs = 512 * G (L1-resident) and waits for
     // the accumulator on its own, so a slow warp does not hold up the others.
     uint32_t local = 0;
+    // fused adler32 (kAdler): this lane's sums of the J bytes it stores,
+    // sum d_i and sum i d_i with the byte position i taken mod 65521
+    unsigned long long ad_s1 = 0, ad_s2 = 0;
     TileCursor cur;
     cur.start<kGrouped>(p);
     for (int tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x, ++local) {
@@ -589,6 +592,13 @@ __global__ void __launch_bounds__(Roles<kEpiW>::kThreads, 1) bf_form_beams_tc(co
       const int64_t bstride = static_cast<int64_t>(P.F) * 2 * P.jpitch;  // bytes between beams, both layouts
       const int blim = P.B - b0 - static_cast<int>(j4);  // beam offsets below this exist
       uint8_t *dst = jrow + static_cast<int64_t>(8 * c_begin) * bstride;  // beam 8 c + j4 of the lane's chunk c
+      // fused adler32: word h of the lane's chunk c_begin + cc sits at byte
+      // position base + cc * step + h * half (mod 65521), so the tile needs only
+      // a0 = sum of its bytes, a1 = sum cc * (bytes of chunk cc), a2 = sum of the
+      // second words' bytes, a3 = sum k * byte_k within words; then
+      // sum i d_i = base a0 + step a1 + half a2 + a3 (32-bit sums per tile:
+      // bytes <= 255, at most 16 words; the products are taken in 64 bits)
+      uint32_t ad_a0 = 0, ad_a1 = 0, ad_a2 = 0, ad_a3 = 0;
 
       auto process = [&](int c, const uint32_t (&r)[16]) {
         const float4 ga = __ldg(reinterpret_cast<const float4 *>(gcur + 8 * c));
@@ -618,6 +628,16 @@ __global__ void __launch_bounds__(Roles<kEpiW>::kThreads, 1) bf_form_beams_tc(co
           if (8 * c < blim) __stcs(reinterpret_cast<uint32_t *>(dst), w[0]);
           if (8 * c + 4 < blim) __stcs(reinterpret_cast<uint32_t *>(dst + 4 * bstride), w[1]);
         }
+        if constexpr (kAdler) {  // only the bytes stored count
+          const uint32_t w0 = (t_ok && 8 * c < blim) ? w[0] : 0u;
+          const uint32_t w1 = (t_ok && 8 * c + 4 < blim) ? w[1] : 0u;
+          const uint32_t s1 = __dp4a(w1, 0x01010101u, 0u);
+          const uint32_t s01 = __dp4a(w0, 0x01010101u, s1);
+          ad_a0 += s01;
+          ad_a1 += static_cast<uint32_t>(c - c_begin) * s01;
+          ad_a2 += s1;
+          ad_a3 = __dp4a(w1, 0x03020100u, __dp4a(w0, 0x03020100u, ad_a3));
+        }
         dst += 8 * bstride;
       };
 
@@ -640,6 +660,27 @@ __global__ void __launch_bounds__(Roles<kEpiW>::kThreads, 1) bf_form_beams_tc(co
       }
       tc_fence_before();
       mbar_arrive(accempty(ab));
+      if constexpr (kAdler) {
+        const uint64_t off = static_cast<uint64_t>((jrow + static_cast<int64_t>(8 * c_begin) * bstride) - P.jbase);
+        const uint32_t base = static_cast<uint32_t>(off % kAdlerMod);
+        const uint32_t half = static_cast<uint32_t>(static_cast<uint64_t>(4 * bstride) % kAdlerMod);
+        const uint32_t step = static_cast<uint32_t>(static_cast<uint64_t>(8 * bstride) % kAdlerMod);
+        ad_s1 += ad_a0;
+        ad_s2 += static_cast<unsigned long long>(base) * ad_a0 + static_cast<unsigned long long>(step) * ad_a1 +
+                 static_cast<unsigned long long>(half) * ad_a2 + ad_a3;
+      }
+    }
+    if constexpr (kAdler) {  // one pair of atomics per warp
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        ad_s1 += __shfl_xor_sync(0xffffffffu, ad_s1, o);
+        ad_s2 += __shfl_xor_sync(0xffffffffu, ad_s2, o);
+      }
+      if (lane == 0) {
+        const TcProblem &P0 = p.one;
+        atomicAdd(P0.adler, ad_s1);
+        atomicAdd(P0.adler + 1, ad_s2);
+      }
     }
   }
 
@@ -812,6 +853,8 @@ static cudaError_t make_problem(TcProblem &P, const TcWeights &w, int64_t T, uin
   P.F = static_cast<int>(F);
   P.B = static_cast<int>(w.B);
   P.J = J;
+  P.jbase = J;
+  P.adler = nullptr;
   P.jpitch = jpitch > 0 ? jpitch : T;
   if (P.jpitch < T || (P.jpitch & 3)) return cudaErrorInvalidValue;
   if (j_layout != kJLinear && j_layout != kJ2) return cudaErrorInvalidValue;
@@ -872,30 +915,39 @@ static cudaError_t plan_launch(TcParams &p, int max_nb_pass, const TcRingPlan &p
   return *smem_bytes > kSmemLimit ? cudaErrorInvalidValue : cudaSuccess;
 }
 
-template <bool kGrouped, bool kJ2, int kEpiW>
+template <bool kGrouped, bool kJ2, int kEpiW, bool kAdler>
 static cudaError_t launch_inst(const TcParams &p, int smem_bytes, cudaStream_t s) {
   static std::atomic<bool> attr_set{false};
   if (!attr_set.load()) {
-    const cudaError_t e = cudaFuncSetAttribute(bf_form_beams_tc<kGrouped, kJ2, kEpiW>,
+    const cudaError_t e = cudaFuncSetAttribute(bf_form_beams_tc<kGrouped, kJ2, kEpiW, kAdler>,
                                                cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
     if (e != cudaSuccess) return e;
     attr_set.store(true);
   }
   const int grid = std::min(p.ntiles, num_sms());
   if (grid <= 0) return cudaSuccess;
-  bf_form_beams_tc<kGrouped, kJ2, kEpiW><<<grid, Roles<kEpiW>::kThreads, smem_bytes, s>>>(p);
+  bf_form_beams_tc<kGrouped, kJ2, kEpiW, kAdler><<<grid, Roles<kEpiW>::kThreads, smem_bytes, s>>>(p);
   return cudaGetLastError();
 }
 
-// Instantiation for a launch: J2 output only in plain launches; the epilogue
-// width by the K stages per tile.
+template <bool kJ2, bool kAdler>
+static cudaError_t launch_plain(const TcParams &p, int smem_bytes, cudaStream_t s) {
+  return p.nk <= 4 ? launch_inst<false, kJ2, 12, kAdler>(p, smem_bytes, s)
+                   : launch_inst<false, kJ2, 8, kAdler>(p, smem_bytes, s);
+}
+
+// Instantiation for a launch: J2 output and the fused adler32 only in plain
+// launches; the epilogue width by the K stages per tile (12 warps up to 4).
 template <bool kGrouped>
 static cudaError_t launch_kernel(const TcParams &p, int smem_bytes, cudaStream_t s) {
-  const bool wide_epi = p.nk <= 4;
-  if (!kGrouped && p.one.jlayout == kJ2)
-    return wide_epi ? launch_inst<false, true, 12>(p, smem_bytes, s) : launch_inst<false, true, 8>(p, smem_bytes, s);
-  return wide_epi ? launch_inst<kGrouped, false, 12>(p, smem_bytes, s)
-                  : launch_inst<kGrouped, false, 8>(p, smem_bytes, s);
+  if constexpr (kGrouped) {
+    return p.nk <= 4 ? launch_inst<true, false, 12, false>(p, smem_bytes, s)
+                     : launch_inst<true, false, 8, false>(p, smem_bytes, s);
+  } else {
+    const bool j2 = p.one.jlayout == kJ2, adler = p.one.adler != nullptr;
+    if (j2) return adler ? launch_plain<true, true>(p, smem_bytes, s) : launch_plain<true, false>(p, smem_bytes, s);
+    return adler ? launch_plain<false, true>(p, smem_bytes, s) : launch_plain<false, false>(p, smem_bytes, s);
+  }
 }
 
 cudaError_t tc_make_problem(TcProblem &P, const TcWeights &w, int64_t T, uint8_t *J, const uint8_t *E,
@@ -922,10 +974,13 @@ cudaError_t launch_tc_grouped(const TcProblem *table, int nprob, int ntiles, int
 }
 
 cudaError_t launch_tc(const TcWeights &w, int64_t T, uint8_t *J, const uint8_t *E, int *err, cudaStream_t s,
-                      int64_t jpitch, int j_layout) {
+                      int64_t jpitch, int j_layout, unsigned long long *adler, const uint8_t *jbase) {
   TcParams p{};
   cudaError_t e = make_problem(p.one, w, T, J, E, jpitch, j_layout);
   if (e != cudaSuccess) return e;
+  p.one.adler = adler;
+  if (jbase) p.one.jbase = jbase;
+  if (adler && (p.one.jbase > J)) return cudaErrorInvalidValue;
   const int64_t ntiles = static_cast<int64_t>(p.one.ntt) * w.F * w.npass;
   if (ntiles > 0x7FFFFFFF) return cudaErrorInvalidValue;
   p.ntiles = static_cast<int>(ntiles);

@@ -366,6 +366,48 @@ def run_ours(args):
     roofline = roofline_of(bf, stream, d.cmacs, alg_bytes, k_ms, "bf_form_beams_tc")
     roofline["traffic"] = profile_traffic()
 
+    # the checksum the reference prints after form_beams (arraysizes.cxx:79):
+    # summed in the kernel's epilogue vs a second pass over J; both calls are
+    # synchronous, so host wall time per call (weight preparation included)
+    fused = bf.form_beams_adler(d, J, E, A, G, stream=stream)
+    torch.cuda.synchronize()
+    t_f, t_s, g_f, g_p, g_a = [], [], [], [], []
+
+    def ev_pair():
+        return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    for _ in range(30):  # the arms interleaved; medians of per-call host wall and device times
+        e0, e1 = ev_pair()
+        t0 = time.perf_counter()
+        e0.record(stream)
+        fused = bf.form_beams_adler(d, J, E, A, G, stream=stream)
+        e1.record(stream)
+        t_f.append(time.perf_counter() - t0)
+        e2, e3 = ev_pair()
+        e4, e5 = ev_pair()
+        t0 = time.perf_counter()
+        e2.record(stream)
+        bf.form_beams_ex(d, J, E, A, G, stream=stream)
+        e3.record(stream)
+        e4.record(stream)
+        separate = bf.adler32_device(J, stream=stream)
+        e5.record(stream)
+        t_s.append(time.perf_counter() - t0)
+        torch.cuda.synchronize()
+        g_f.append(e0.elapsed_time(e1))
+        g_p.append(e2.elapsed_time(e3))
+        g_a.append(e4.elapsed_time(e5))
+    assert fused == separate == checksum
+    med = statistics.median
+    checksum_block = {
+        "adler32": f"0x{fused:08x}",
+        "fused_ms": round(1e3 * med(t_f), 4),
+        "separate_pass_ms": round(1e3 * med(t_s), 4),
+        "device_ms": {"form_beams_with_fused_sums": round(med(g_f), 4), "form_beams": round(med(g_p), 4),
+                      "adler32_pass": round(med(g_a), 4)},
+        "api": "bf_form_beams_adler vs bf_form_beams_ex + bf_adler32_device, device buffers; host wall and CUDA events",
+    }
+
     e2e = None
     if not args.no_e2e:
         Eh = torch.empty(d.esize, dtype=torch.uint8, pin_memory=True)
@@ -424,6 +466,7 @@ def run_ours(args):
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": e2e,
+            "checksum": checksum_block,
             "clocks": clk,
             "gpu_launches": 2 * args.steps,
         }

@@ -188,6 +188,17 @@ typedef enum bf_j_layout { BF_J_LINEAR = 0, BF_J_J2 = 1 } bf_j_layout;
 BF_API int bf_form_beams_layout(const bf_dims *dims, uint8_t *J, const uint8_t *E, const uint8_t *A, const float *G,
                                 int a_layout, int j_layout, int ptr_kind, bf_stream_t stream);
 
+/* bf_form_beams_layout that also returns in *adler the adler32 (adler32.c:7-20)
+ * of the whole J it wrote, jsize bytes in j_layout: the checksum the
+ * reference's main() computes after form_beams (arraysizes.cxx:79), without a
+ * second pass over J.  The tensor-core kernel sums the bytes it stores (two
+ * dp4a per 4 bytes, positions mod 65521) and a host step finishes
+ * a = 1 + sum d_i, b = n + n sum d_i - sum i d_i; when the dp4a kernel runs
+ * instead, J is checksummed by bf_adler32_device's pass.  Synchronous for
+ * both pointer kinds: *adler is set when it returns BF_OK. */
+BF_API int bf_form_beams_adler(const bf_dims *dims, uint8_t *J, const uint8_t *E, const uint8_t *A, const float *G,
+                               int a_layout, int j_layout, int ptr_kind, uint32_t *adler, bf_stream_t stream);
+
 /* Measures the dense E4M3 tensor-core rate of the current device, in
  * TFLOP/s (two flops per multiply-add): every SM issues back-to-back
  * tcgen05 MMAs of the kind the beamformer uses (M=128, N=256, K=32, A operand

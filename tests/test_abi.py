@@ -27,6 +27,14 @@ def test_library_exports_every_symbol(bflib):
         assert hasattr(L, name), name
 
 
+def test_every_binding_declares_its_arguments(bflib):
+    """Without argtypes ctypes passes Python ints as 32-bit C ints, which cuts
+    64-bit addresses; every entry point the package binds declares them."""
+    L = bflib.lib()
+    for name in bflib.EXPORTED_SYMBOLS:
+        assert getattr(L, name).argtypes is not None, name
+
+
 def test_status_strings(bflib):
     L = bflib.lib()
     for code in range(0, 9):
@@ -66,6 +74,11 @@ def test_invalid_arguments(bflib):
     assert L.bf_form_beams_ex(ctypes.byref(d0), None, None, None, None, 0, None) == bflib.OK
     out = ctypes.c_uint32()
     assert L.bf_adler32_device(None, 0, ctypes.byref(out), None) == bflib.OK and out.value == 1
+    # the checksummed call wants somewhere to put the checksum; an empty problem's is 1
+    assert L.bf_form_beams_adler(ctypes.byref(d0), None, None, None, None, 0, 0, 0, None, None) == (
+        bflib.ERR_INVALID_ARGUMENT)
+    assert L.bf_form_beams_adler(ctypes.byref(d0), None, None, None, None, 0, 0, 0, ctypes.byref(out), None) == bflib.OK
+    assert out.value == 1
     # layouts are checked before any device work
     dl = bflib.Dims(16, 1, 128, 2, 8).c()
     assert L.bf_form_beams_layout(ctypes.byref(dl), J.ctypes.data, J.ctypes.data, J.ctypes.data, J.ctypes.data, 2, 0,
