@@ -207,10 +207,56 @@ int64_t chunk_times(const bf_dims &d) {
   return tc * 3 / 2 >= d.ntimes ? d.ntimes : tc;
 }
 
+int num_sms_api() {
+  static const int n = [] {
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      v = 1;
+    return v > 0 ? v : 1;
+  }();
+  return n;
+}
+
+// Copies bytes [off, off + len) of each of `rows` rows (`pitch` bytes apart)
+// from the device J to the caller's J in pinned host memory (its device
+// mapping): one 16-byte load and streaming store per step, so a warp writes
+// whole 64-byte lines across the host link.  off, len, pitch and both base
+// addresses are multiples of 16.
+__global__ void __launch_bounds__(256) drain_rows(const uint8_t *__restrict__ src, uint8_t *__restrict__ dst,
+                                                  int64_t rows, int64_t pitch, int64_t off, int64_t len) {
+  const int64_t per_row = len / 16;
+  const int64_t total = rows * per_row;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int64_t r = i / per_row;
+    const int64_t o = r * pitch + off + 16 * (i - r * per_row);
+    __stcs(reinterpret_cast<uint4 *>(dst + o), __ldcs(reinterpret_cast<const uint4 *>(src + o)));
+  }
+}
+
+// Device address of the caller's J when it is pinned host memory that the
+// drain can write directly (16-byte aligned, rows a multiple of 16 bytes);
+// null otherwise (pageable memory: one copy at the end instead).
+uint8_t *mapped_host_j(uint8_t *J, const bf_dims &d, int j_layout) {
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, J) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return nullptr;
+  }
+  const int64_t pitch = j_layout == kJ2 ? d.ntimes * d.npolarizations : d.ntimes;
+  if (at.type != cudaMemoryTypeHost || !at.devicePointer || (pitch & 15) ||
+      (reinterpret_cast<uintptr_t>(at.devicePointer) & 15))
+    return nullptr;
+  return static_cast<uint8_t *>(at.devicePointer);
+}
+
 // Host-pointer pass pipelined over time chunks: E[t0..t1][f][d][p] is
 // contiguous, so each chunk goes in with one copy on one of kLanes streams and
 // is beamformed while the next chunk copies; every chunk writes its times of J
-// (rows of ntimes bytes) in a device buffer that is copied out once at the end.
+// (rows of ntimes bytes) in a device buffer.  When the caller's J is pinned,
+// a drain kernel behind each chunk writes the chunk's row segments straight
+// into it, so J leaves over the link while later chunks of E arrive;
+// otherwise J is copied out once at the end.
 // A, G and the tensor-core operand are uploaded / prepared once.  Synchronous;
 // the caller holds c.mu.
 int run_host_pipelined(DeviceCtx &c, const bf_dims &d, uint8_t *J, const uint8_t *E, const uint8_t *A,
@@ -255,6 +301,11 @@ int run_host_pipelined(DeviceCtx &c, const bf_dims &d, uint8_t *J, const uint8_t
   BF_TRY(cudaEventRecord(l0.done, l0.s));
   for (int i = 1; i < kLanes; ++i) BF_TRY(cudaStreamWaitEvent(c.lanes[i].s, l0.done, 0));
   t_last_kernel = use_tc ? "tensor" : "simt";
+  uint8_t *jmap = mapped_host_j(J, d, j_layout);
+  const int64_t P = d.npolarizations;
+  const int64_t jrows = j_layout == kJ2 ? d.nbeams * d.nfrequencies : d.nbeams * d.nfrequencies * P;
+  const int64_t jpitch = j_layout == kJ2 ? T * P : T;
+  const int64_t jscale = j_layout == kJ2 ? P : 1;  // bytes per time in a row
   for (int64_t t0 = 0, k = 0; t0 < T; t0 += tc, ++k) {
     Lane &l = c.lanes[k % kLanes];
     const int64_t nt = std::min(tc, T - t0);
@@ -268,12 +319,17 @@ int run_host_pipelined(DeviceCtx &c, const bf_dims &d, uint8_t *J, const uint8_t
       const bf_dims dc{nt, d.nfrequencies, d.ndishes, d.npolarizations, d.nbeams};
       BF_TRY(launch_simt(dc, Jc, l.E.as<uint8_t>(), c.A.as<uint8_t>(), c.G.as<float>(), l.s, T, a_layout, j_layout));
     }
+    if (jmap) {
+      const int grid = 2 * std::max(1, num_sms_api());
+      drain_rows<<<grid, 256, 0, l.s>>>(c.J.as<uint8_t>(), jmap, jrows, jpitch, t0 * jscale, nt * jscale);
+      BF_TRY(cudaGetLastError());
+    }
   }
   for (int i = 1; i < kLanes; ++i) {
     BF_TRY(cudaEventRecord(c.lanes[i].done, c.lanes[i].s));
     BF_TRY(cudaStreamWaitEvent(l0.s, c.lanes[i].done, 0));
   }
-  BF_TRY(cudaMemcpyAsync(J, c.J.p, jsize(d), cudaMemcpyDeviceToHost, l0.s));
+  if (!jmap) BF_TRY(cudaMemcpyAsync(J, c.J.p, jsize(d), cudaMemcpyDeviceToHost, l0.s));
   BF_TRY(cudaStreamSynchronize(l0.s));
   return read_and_clear_err(c, caller);
 }
