@@ -114,22 +114,51 @@ struct TcParams {
   int *err;
 };
 
-// Problem of a tile and the tile's index inside it.
-template <bool kGrouped>
-__device__ __forceinline__ const TcProblem &problem_of(const TcParams &p, int tile, int &lt) {
-  if constexpr (!kGrouped) {
-    lt = tile;
-    return p.one;
-  } else {
-    int lo = 0, hi = p.nprob - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (p.table[mid].tile_begin <= tile) lo = mid; else hi = mid - 1;
+// Tiles of a CTA.  A plain launch strides them over the grid.  A grouped
+// launch gives each CTA a contiguous range, so that it stays with one problem
+// for many tiles: every change of problem costs each role a tensor-map
+// acquire and a cold descriptor, and with strided tiles almost every tile of
+// a large batch belongs to another problem.
+struct TileRange {
+  int first, end, step;
+  template <bool kGrouped>
+  __device__ __forceinline__ static TileRange of(const TcParams &p) {
+    if constexpr (kGrouped) {
+      const int64_t n = p.ntiles, g = gridDim.x, b = blockIdx.x;
+      return {static_cast<int>(b * n / g), static_cast<int>((b + 1) * n / g), 1};
+    } else {
+      return {static_cast<int>(blockIdx.x), p.ntiles, static_cast<int>(gridDim.x)};
     }
-    lt = tile - p.table[lo].tile_begin;
-    return p.table[lo];
   }
-}
+  __device__ __forceinline__ uint32_t count() const {
+    return first < end ? static_cast<uint32_t>((end - 1 - first) / step + 1) : 0u;
+  }
+};
+
+// Problem of a tile and the tile's index inside it; a CTA's tiles only grow,
+// so a grouped launch walks the table forward from the last problem seen.
+template <bool kGrouped>
+struct ProblemCursor {
+  int idx = -1;
+  __device__ __forceinline__ const TcProblem &at(const TcParams &p, int tile, int &lt) {
+    if constexpr (!kGrouped) {
+      lt = tile;
+      return p.one;
+    } else {
+      if (idx < 0) {  // first tile: binary search
+        int lo = 0, hi = p.nprob - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (p.table[mid].tile_begin <= tile) lo = mid; else hi = mid - 1;
+        }
+        idx = lo;
+      }
+      while (idx + 1 < p.nprob && p.table[idx + 1].tile_begin <= tile) ++idx;
+      lt = tile - p.table[idx].tile_begin;
+      return p.table[idx];
+    }
+  }
+};
 
 // Coordinates (beam pass, 64-time block, frequency) of a CTA's tiles.  A plain
 // launch visits tiles blockIdx.x, + gridDim.x, ...: the cursor adds the grid
@@ -320,9 +349,11 @@ __global__ void __launch_bounds__(Roles<kEpiW>::kThreads, 1) bf_form_beams_tc(co
       const TcProblem *seen = nullptr;
       TileCursor cur;
       cur.start<kGrouped>(p);
-      for (int tile = blockIdx.x; ok && tile < p.ntiles; tile += gridDim.x) {
+      const TileRange tr = TileRange::of<kGrouped>(p);
+      ProblemCursor<kGrouped> pc;
+      for (int tile = tr.first; ok && tile < tr.end; tile += tr.step) {
         int lt;
-        const TcProblem &P = problem_of<kGrouped>(p, tile, lt);
+        const TcProblem &P = pc.at(p, tile, lt);
         if (kGrouped && &P != seen) {  // a table entry the host rewrites between launches
           tensormap_acquire(&P.tm_e);
           seen = &P;
@@ -358,9 +389,11 @@ __global__ void __launch_bounds__(Roles<kEpiW>::kThreads, 1) bf_form_beams_tc(co
       const TcProblem *seen = nullptr;
       TileCursor cur;
       cur.start<kGrouped>(p);
-      for (int tile = blockIdx.x; ok && tile < p.ntiles; tile += gridDim.x) {
+      const TileRange tr = TileRange::of<kGrouped>(p);
+      ProblemCursor<kGrouped> pc;
+      for (int tile = tr.first; ok && tile < tr.end; tile += tr.step) {
         int lt;
-        const TcProblem &P = problem_of<kGrouped>(p, tile, lt);
+        const TcProblem &P = pc.at(p, tile, lt);
         if (kGrouped && &P != seen) {  // a table entry the host rewrites between launches
           tensormap_acquire(&P.tm_w);
           tensormap_acquire(&P.tm_d);
@@ -409,9 +442,11 @@ __global__ void __launch_bounds__(Roles<kEpiW>::kThreads, 1) bf_form_beams_tc(co
       const uint64_t w_desc0 = smem_desc_sw128(smem_u32(sW));
       uint32_t local = 0;
       bool ok = true;
-      for (int tile = blockIdx.x; ok && tile < p.ntiles; tile += gridDim.x, ++local) {
+      const TileRange tr = TileRange::of<kGrouped>(p);
+      ProblemCursor<kGrouped> pc;
+      for (int tile = tr.first; ok && tile < tr.end; tile += tr.step, ++local) {
         int lt;
-        const TcProblem &P = problem_of<kGrouped>(p, tile, lt);
+        const TcProblem &P = pc.at(p, tile, lt);
         const uint32_t idesc = idesc_e4m3_f32(kBM, 2 * P.nb_pass);
         const int wbox = 2 * P.nb_pass * kKC;
         const uint32_t ab = local & 1u;
@@ -454,9 +489,8 @@ __global__ void __launch_bounds__(Roles<kEpiW>::kThreads, 1) bf_form_beams_tc(co
     const uint32_t tl = 16u * q + (lane >> 1);
     const uint32_t lane_addr = static_cast<uint32_t>(32 * q) << 16;
     const uint32_t sel = pp ? 0x7531u : 0x6420u;  // odd or even bytes: polarization 1 or 0
-    // this CTA's K stages: tiles blockIdx.x, blockIdx.x + gridDim.x, ... times nk
-    const uint32_t my_tiles =
-        static_cast<int>(blockIdx.x) < p.ntiles ? (p.ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0u;
+    // this CTA's K stages: its tiles (TileRange) times nk
+    const uint32_t my_tiles = TileRange::of<kGrouped>(p).count();
     const uint32_t total = my_tiles * static_cast<uint32_t>(p.nk);
     // W slots: the tensor core's release of an operand stage (empty) also ends
     // its use of that stage's W slot, so the lead lane of the group handling
@@ -549,9 +583,11 @@ __global__ void __launch_bounds__(Roles<kEpiW>::kThreads, 1) bf_form_beams_tc(co
     unsigned long long ad_s1 = 0, ad_s2 = 0;
     TileCursor cur;
     cur.start<kGrouped>(p);
-    for (int tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x, ++local) {
+    const TileRange tr = TileRange::of<kGrouped>(p);
+    ProblemCursor<kGrouped> pc;
+    for (int tile = tr.first; tile < tr.end; tile += tr.step, ++local) {
       int lt;
-      const TcProblem &P = problem_of<kGrouped>(p, tile, lt);
+      const TcProblem &P = pc.at(p, tile, lt);
       int pass, tt, f;
       cur.take<kGrouped>(P, lt, pass, tt, f);
       const int nchunk = P.nb_pass / 8;
