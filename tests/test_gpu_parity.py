@@ -106,14 +106,31 @@ def test_pattern_golden_small(bflib, cuda):
         assert zlib.adler32(J.tobytes()) == 0xAB69DFEE, kernel
 
 
-def test_pattern_golden_production_shape(bflib, cuda):
-    """setup() pattern at t=32768, f=16, b=96: checksum 0x27303ea9 (arraysizes.cxx:54)."""
+# setup() pattern shapes with the reference's checksums (arraysizes.cxx:54-57:
+# 0x27303ea9, 0xc4fb6a4c, 0x4de6498f) and the ones its program printed here
+PATTERN_SHAPES = [
+    (32768, 16, 512, 2, 96),
+    (32768, 32, 512, 2, 96),
+    (32768, 32, 512, 2, 128),
+    (2048, 16, 512, 2, 96),
+    (8, 32, 512, 2, 128),
+    (1, 32, 512, 2, 128),
+]
+
+
+@pytest.mark.parametrize("shape", PATTERN_SHAPES)
+def test_pattern_goldens(bflib, cuda, golden, shape):
+    """setup() pattern inputs give the reference's checksums (t = 8 and 1 run on
+    the dp4a kernel, the others on the tensor cores; b = 128 in two passes)."""
     from oracle import oracle as O
 
-    d = bflib.Dims(32768, 16, 512, 2, 96)
-    E, A, G = O.setup_pattern(O.Dims(32768, 16, 512, 2, 96))
-    J = run_gpu(bflib, cuda, d, E, A, G, "tensor")
-    assert zlib.adler32(J.tobytes()) == 0x27303EA9
+    g, _ = golden
+    rec = next(r for r in g["pattern"] if (r["T"], r["F"], r["D"], r["P"], r["B"]) == shape)
+    d = bflib.Dims(*shape)
+    E, A, G = O.setup_pattern(O.Dims(*shape))
+    J = run_gpu(bflib, cuda, d, E, A, G)
+    assert bflib.last_kernel() == ("tensor" if shape[0] % 16 == 0 else "simt")
+    assert zlib.adler32(J.tobytes()) == rec["adler32"]
 
 
 def test_plain_beamform_workload_drop_in(bflib, cuda, golden):
