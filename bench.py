@@ -95,6 +95,17 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
+def bf16_peak():
+    """(dense bf16 TFLOP/s burst, kind) from the measured peaks, else the fallback."""
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fp:
+            p = json.load(fp)
+        if "bf16_tflops" in p:
+            return float(p["bf16_tflops"]), "measured"
+    return 1900.0, "fallback"
+
+
 def profile_traffic():
     """DRAM bytes per launch of the tensor-core kernel from the committed ncu summary."""
     if not os.path.exists(PROFILE_SUMMARY):
@@ -275,9 +286,14 @@ def roofline_of(bf, stream, cmacs, alg_bytes, k_ms, kernel):
     t_tc = 8 * cmacs / (tc_peak * 1e12)
     hbm = {"achieved": round(alg_bytes / k_s / 1e9, 1), "peak": hbm_peak, "unit": "GB/s",
            "frac": round(t_hbm / k_s, 4), "peak_kind": f"{hbm_kind} (copy bandwidth)"}
+    bf16, bf16_kind = bf16_peak()
     tensor = {"achieved": round(8 * cmacs / k_s / 1e12, 1), "peak": round(tc_peak, 1), "unit": "TFLOP/s",
               "frac": round(t_tc / k_s, 4),
-              "peak_kind": "measured in this run: dense E4M3 tcgen05 MMA stream on every SM (bf_tensor_peak)"}
+              "peak_kind": "measured in this run: dense E4M3 tcgen05 MMA stream on every SM (bf_tensor_peak)",
+              # the same achieved rate against twice the cuBLAS bf16 burst of the
+              # peaks file (dense fp8 runs at twice the bf16 rate)
+              "vs_2x_bf16": {"peak": round(2 * bf16, 1), "frac": round(8 * cmacs / k_s / 1e12 / (2 * bf16), 4),
+                             "peak_kind": f"{bf16_kind} bf16 x 2"}}
     bound = "hbm" if t_hbm >= t_tc else "tensor"
     main = hbm if bound == "hbm" else tensor
     return {"bound": bound, "kernel": kernel, **main, "kernel_ms": round(k_ms, 4), "algorithmic_bytes": alg_bytes,
