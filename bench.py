@@ -273,6 +273,23 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def max_over_ranks(ms, dist, device):
+    """The step time of the whole job: the slowest replica's (max over ranks
+    of the per-rank time, all-reduced on `device`; `dist` None for one rank)."""
+    import torch
+
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(cmacs_per_rank, world, ms_max):
+    """Whole-job throughput of `world` replicas that each process
+    `cmacs_per_rank` complex MACs per step of `ms_max` milliseconds."""
+    return cmacs_per_rank * world / (ms_max * 1e-3)
+
+
 def roofline_of(bf, stream, cmacs, alg_bytes, k_ms, kernel):
     """Both rooflines of a tensor-core launch: HBM (algorithmic bytes against
     the measured copy bandwidth) and tensor (8 flops per complex MAC -- the
@@ -356,11 +373,8 @@ def run_ours(args):
     ms = ev0.elapsed_time(ev1) / args.steps
     clk = clocks.stop() if rank == 0 else None
     bf.stream_status(stream)
-    ms_t = torch.tensor([ms], device="cuda")
-    if dist is not None:
-        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
-    ms_max = float(ms_t.item())
-    value = d.cmacs * world / (ms_max * 1e-3)
+    ms_max = max_over_ranks(ms, dist, "cuda")
+    value = job_value(d.cmacs, world, ms_max)
 
     # dominant kernel alone: resident weights, one tensor-core launch per event pair
     W = bf.ResidentWeights(d.nfrequencies, d.nbeams, d.ndishes, A, G, stream=stream)
