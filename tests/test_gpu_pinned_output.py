@@ -61,3 +61,16 @@ def test_pinned_and_pageable_J_agree(bflib, cuda):
     bflib.form_beams_ex(d, Jp, E, A, G)
     bflib.form_beams_ex(d, Jh, E, A, G)
     np.testing.assert_array_equal(Jp, Jh)
+
+
+def test_pinned_J_with_unaligned_rows_falls_back(bflib, cuda, oracle, monkeypatch):
+    """Rows of T = 200 bytes are not a multiple of 16: the drain cannot write
+    them with 16-byte stores, so J is copied out once at the end (the dp4a
+    kernel takes this T)."""
+    monkeypatch.setenv("BF_HOST_CHUNK_BYTES", str(64 * 2 * 64 * 2))
+    d = bflib.Dims(200, 2, 64, 2, 24)
+    E, A, G = bflib.seeded_host_inputs(d, 41)
+    J = _pinned(cuda, d.jsize)
+    J[:] = 0x5A
+    bflib.form_beams_ex(d, J, E, A, G)
+    np.testing.assert_array_equal(J, _oracle_J(oracle, d, E, A, G, "linear"))
