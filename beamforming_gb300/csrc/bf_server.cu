@@ -30,8 +30,6 @@ namespace {
 using namespace bf;
 using Clock = std::chrono::steady_clock;
 
-double seconds(Clock::time_point t) { return std::chrono::duration<double>(t.time_since_epoch()).count(); }
-
 // First-fit allocator over one device arena (offsets aligned to 256 bytes).
 class Pool {
  public:
