@@ -395,14 +395,14 @@ class ResidentWeights:
 
 class _ServerConfig(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_int64), ("max_batch", ctypes.c_int), ("max_inflight", ctypes.c_int),
-                ("spin_wait", ctypes.c_int)]
+                ("spin_wait", ctypes.c_int), ("staging_bytes", ctypes.c_int64)]
 
 
 class _ServerStats(ctypes.Structure):
     _fields_ = [
         (n, ctypes.c_int64)
         for n in ("submitted", "completed", "batches", "chunks_launched", "max_batch_seen", "pool_bytes",
-                  "pool_peak_bytes", "weight_updates")
+                  "pool_peak_bytes", "weight_updates", "staged")
     ]
 
 
@@ -410,13 +410,14 @@ class Server:
     """Continuous-batching server over resident weights: ``submit`` chunks as
     they arrive, ``wait`` for a ticket (latency in seconds), ``drain``.  The
     server reads E and writes J after ``submit`` returns; the wrapper keeps
-    the buffers referenced until the ticket is waited for (host buffers
-    should be pinned for the copies to overlap)."""
+    the buffers referenced until the ticket is waited for.  Pageable host
+    buffers go through the server's pinned staging ring (``staging_bytes``;
+    0: 256 MiB, negative: none), pinned ones are copied directly."""
 
     def __init__(self, weights: "ResidentWeights", hbm_budget_bytes: int = 0, max_batch: int = 0,
-                 max_inflight: int = 0, spin_wait: bool = False):
+                 max_inflight: int = 0, spin_wait: bool = False, staging_bytes: int = 0):
         self.weights = weights
-        cfg = _ServerConfig(hbm_budget_bytes, max_batch, max_inflight, int(spin_wait))
+        cfg = _ServerConfig(hbm_budget_bytes, max_batch, max_inflight, int(spin_wait), staging_bytes)
         h = ctypes.c_void_p()
         _check(lib().bf_server_create(ctypes.byref(h), weights._h, ctypes.byref(cfg)), "bf_server_create")
         self._h = h

@@ -17,6 +17,7 @@
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
+#include <cstring>
 #include <deque>
 #include <map>
 #include <memory>
@@ -30,17 +31,21 @@ namespace {
 using namespace bf;
 using Clock = std::chrono::steady_clock;
 
-// First-fit allocator over one device arena (offsets aligned to 256 bytes).
+// First-fit allocator over one arena (offsets aligned to 256 bytes): device
+// memory for chunk buffers, or pinned host memory for the staging ring.
 class Pool {
  public:
-  bool init(size_t bytes) {
-    if (cudaMalloc(&base_, bytes) != cudaSuccess) return false;
+  bool init(size_t bytes, bool host = false) {
+    host_ = host;
+    void *p = nullptr;
+    if ((host ? cudaMallocHost(&p, bytes) : cudaMalloc(&p, bytes)) != cudaSuccess) return false;
+    base_ = static_cast<uint8_t *>(p);
     size_ = bytes;
     free_[0] = bytes;
     return true;
   }
   ~Pool() {
-    if (base_) cudaFree(base_);
+    if (base_) (void)(host_ ? cudaFreeHost(base_) : cudaFree(base_));
   }
   uint8_t *alloc(size_t n) {
     n = (n + 255) / 256 * 256;
@@ -78,9 +83,21 @@ class Pool {
 
  private:
   uint8_t *base_ = nullptr;
+  bool host_ = false;
   size_t size_ = 0, used_ = 0;
   std::map<size_t, size_t> free_;
 };
+
+// Host memory the copy engines read and write asynchronously (pinned or
+// registered); pageable memory answers cudaMemoryTypeUnregistered.
+bool pinned_host(const void *p) {
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeHost;
+}
 
 struct Request {
   int64_t ticket;
@@ -94,6 +111,9 @@ struct Request {
   // set on admission
   uint8_t *dE = nullptr, *dJ = nullptr;
   size_t e_bytes = 0, j_bytes = 0;
+  // pinned staging of pageable host buffers: E was copied into sE at submit
+  // (E then points there); J lands in sJ and is copied to J_user on landing
+  uint8_t *sE = nullptr, *sJ = nullptr, *J_user = nullptr;
 };
 
 // One launch slot: a stream, its problem table and the chunks it carries.
@@ -129,6 +149,7 @@ struct bf_server {
   const bf_weights *weights = nullptr;
   bf_server_config cfg{};
   Pool pool;
+  Pool staging;  // pinned host ring for pageable chunk buffers (may be empty)
   std::vector<std::unique_ptr<Flight>> flights;
   Version ver[kMaxVersions];
   int cur = 0;                      // version new chunks are submitted under
@@ -228,7 +249,14 @@ void bf_server::finish_locked(Flight &fl) {
     --ver[r.version].refs;
     if (!r.e_on_device) pool.release(r.dE, r.e_bytes);
     if (!r.j_on_device) pool.release(r.dJ, r.j_bytes);
-    done_latency[r.ticket] = std::chrono::duration<double>(fl.landed_at - r.arrival).count();
+    Clock::time_point landed = fl.landed_at;
+    if (r.sJ) {  // the chunk's J is in the ring: hand it to the caller's buffer
+      std::memcpy(r.J_user, r.sJ, r.j_bytes);
+      staging.release(r.sJ, r.j_bytes);
+      landed = Clock::now();
+    }
+    if (r.sE) staging.release(r.sE, r.e_bytes);
+    done_latency[r.ticket] = std::chrono::duration<double>(landed - r.arrival).count();
     ++completed;
   }
   fl.reqs.clear();
@@ -352,6 +380,9 @@ int bf_server_create(bf_server **out, const bf_weights *weights, const bf_server
   budget = std::min(budget, free_b * 9 / 10);
   s->cfg.hbm_budget_bytes = static_cast<int64_t>(budget);
   if (st == BF_OK && !s->pool.init(budget)) st = BF_ERR_OUT_OF_MEMORY;
+  if (s->cfg.staging_bytes == 0) s->cfg.staging_bytes = int64_t(256) << 20;
+  if (st == BF_OK && s->cfg.staging_bytes > 0 && !s->staging.init(static_cast<size_t>(s->cfg.staging_bytes), true))
+    st = BF_ERR_OUT_OF_MEMORY;
   if (st == BF_OK && cudaStreamCreateWithFlags(&s->upd_stream, cudaStreamNonBlocking) != cudaSuccess)
     st = BF_ERR_CUDA;
   for (int i = 0; st == BF_OK && i < s->cfg.max_inflight; ++i) {
@@ -399,10 +430,42 @@ int bf_server_submit(bf_server *s, int channel, int nchannels, int64_t ntimes, c
   // a chunk whose buffers can never fit the pool is refused instead of waiting forever
   if ((r.e_on_device ? 0 : r.e_bytes + 256) + (r.j_on_device ? 0 : r.j_bytes + 256) > s->pool.size())
     return BF_ERR_OUT_OF_MEMORY;
-  r.arrival = Clock::now();
+  r.arrival = Clock::now();  // latency includes waiting for ring room and the staging copy
+  // pageable host buffers go through the pinned ring (when they fit in it):
+  // room is taken here, waiting for landed chunks to free it if need be, and
+  // E is copied in by this thread, so the server's device copies stay
+  // asynchronous; J is copied out of the ring when the chunk lands
+  const bool stage_e = !r.e_on_device && !pinned_host(E);
+  const bool stage_j = !r.j_on_device && !pinned_host(J);
+  const size_t need = (stage_e ? r.e_bytes + 256 : 0) + (stage_j ? r.j_bytes + 256 : 0);
+  if (need > 0 && need <= s->staging.size()) {
+    std::unique_lock<std::mutex> lk(s->mu);
+    for (;;) {
+      if (s->status != BF_OK) return s->status;
+      r.sE = stage_e ? s->staging.alloc(r.e_bytes) : nullptr;
+      r.sJ = stage_j && (r.sE || !stage_e) ? s->staging.alloc(r.j_bytes) : nullptr;
+      if ((r.sE || !stage_e) && (r.sJ || !stage_j)) break;
+      if (r.sE) s->staging.release(r.sE, r.e_bytes);  // not both: give back and wait for a landing
+      r.sE = r.sJ = nullptr;
+      s->cv_done.wait_for(lk, std::chrono::milliseconds(50));
+    }
+    ++s->stats.staged;
+  }
+  if (r.sE) {
+    std::memcpy(r.sE, E, r.e_bytes);
+    r.E = r.sE;
+  }
+  if (r.sJ) {
+    r.J_user = J;
+    r.J = r.sJ;
+  }
   {
     std::lock_guard<std::mutex> lk(s->mu);
-    if (s->status != BF_OK) return s->status;
+    if (s->status != BF_OK) {
+      if (r.sE) s->staging.release(r.sE, r.e_bytes);
+      if (r.sJ) s->staging.release(r.sJ, r.j_bytes);
+      return s->status;
+    }
     r.ticket = s->next_ticket++;
     r.version = s->cur;
     ++s->ver[s->cur].refs;

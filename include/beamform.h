@@ -224,6 +224,10 @@ typedef struct bf_server_config {
   int max_inflight;         /* launches in flight; 0: 3 */
   int spin_wait;            /* 1: the server thread polls launches instead of sleeping until a host
                                callback wakes it (lower latency; keeps one host core busy) */
+  int64_t staging_bytes;    /* pinned host ring for chunks whose host buffers are pageable: the
+                               submitting thread copies E into it, the server copies J out of it
+                               when the chunk lands, so the device copies stay asynchronous;
+                               0: 256 MiB, < 0: none (pageable buffers are copied directly) */
 } bf_server_config;
 
 typedef struct bf_server_stats {
@@ -231,6 +235,7 @@ typedef struct bf_server_stats {
   int64_t batches, chunks_launched, max_batch_seen;
   int64_t pool_bytes, pool_peak_bytes;
   int64_t weight_updates;
+  int64_t staged;           /* chunks whose E or J went through the pinned staging ring */
 } bf_server_stats;
 
 /* Creates a server over resident weights (all channels = the weights' frequencies). */

@@ -126,3 +126,57 @@ def test_server_rejects_bad_chunks(bflib, weights):
         srv.submit(0, 40, E, J)  # ntimes not a multiple of 16
     assert ei.value.status == bflib.ERR_UNSUPPORTED
     srv.close()
+
+
+def _pinned_copy(cuda, a):
+    p = cuda.empty(a.size, dtype=cuda.uint8, pin_memory=True).numpy()
+    p[:] = a
+    return p
+
+
+@pytest.mark.parametrize("mode", ["pageable", "pinned", "no_ring"])
+def test_server_pinned_staging_ring(bflib, cuda, oracle, weights, mode):
+    """Pageable host buffers go through the server's pinned staging ring (E
+    copied in at submit, J copied out on landing); pinned buffers and a server
+    without a ring are copied directly.  All give the oracle's bytes."""
+    W, A, G = weights
+    chunks = _chunks(bflib, 12, 9)
+    srv = bflib.Server(W, max_batch=4, max_inflight=2, staging_bytes=-1 if mode == "no_ring" else 0)
+    tickets, outs = [], []
+    for c0, nch, T, E in chunks:
+        J = np.full(B * nch * 2 * T, 0x5A, np.uint8)
+        if mode == "pinned":
+            E, J = _pinned_copy(cuda, E), _pinned_copy(cuda, J)
+        tickets.append(srv.submit(c0, T, E, J, nchannels=nch))
+        outs.append(J)
+    for t in tickets:
+        srv.wait(t)
+    st = srv.stats()
+    srv.close()
+    assert st["staged"] == (len(chunks) if mode == "pageable" else 0)
+    for (c0, nch, T, E), J in zip(chunks, outs):
+        np.testing.assert_array_equal(J, _expected(oracle, A, G, c0, nch, T, E), err_msg=f"{mode} {c0} {nch} {T}")
+
+
+def test_server_small_staging_ring_back_pressure(bflib, oracle, weights):
+    """A ring that holds about two chunks: one thread submitting many chunks
+    without waiting blocks in submit until landed chunks free the ring, and
+    every chunk still comes back right (no wait on the client is needed for
+    the ring to drain)."""
+    W, A, G = weights
+    chunks = _chunks(bflib, 10, 11, sizes=(1024,))
+    per_chunk = max(1024 * nch * D * 2 + B * nch * 2 * 1024 for _, nch, _, _ in chunks) + 512
+    srv = bflib.Server(W, max_batch=2, max_inflight=2, staging_bytes=2 * per_chunk + 4096)
+    tickets, outs = [], []
+    for c0, nch, T, E in chunks:
+        J = np.full(B * nch * 2 * T, 0x5A, np.uint8)
+        tickets.append(srv.submit(c0, T, E, J, nchannels=nch))
+        outs.append(J)
+    srv.drain()
+    for t in tickets:
+        srv.wait(t)
+    st = srv.stats()
+    srv.close()
+    assert st["staged"] == len(chunks)
+    for (c0, nch, T, E), J in zip(chunks, outs):
+        np.testing.assert_array_equal(J, _expected(oracle, A, G, c0, nch, T, E))
