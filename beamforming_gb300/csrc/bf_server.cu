@@ -11,6 +11,9 @@
 // output copy included); a host function queued behind each launch's output
 // copies stamps that moment and wakes the server thread.  max_batch = 1 with
 // max_inflight = 1 is the plain per-chunk loop the server is compared against.
+// Pageable host buffers go through a pinned staging ring: the submitting
+// thread copies E in, the server copies J out when the chunk lands, so the
+// device copies of every chunk are asynchronous.
 #include "bf_internal.h"
 
 #include <algorithm>

@@ -242,9 +242,12 @@ typedef struct bf_server_stats {
 BF_API int bf_server_create(bf_server **out, const bf_weights *weights, const bf_server_config *config);
 
 /* Submits one chunk: channels [channel, channel + nchannels) of ntimes samples,
- * E[t][c][d][p] and J[b][c][p][t] in host memory (pinned for overlap) or device
- * memory (e_on_device / j_on_device).  Returns at once with a ticket; the
- * arrival time is now.  Needs ntimes % 16 == 0. */
+ * E[t][c][d][p] and J[b][c][p][t] in host memory or device memory
+ * (e_on_device / j_on_device).  Pinned host buffers are copied directly;
+ * pageable ones go through the server's pinned staging ring, so this call
+ * copies E into the ring first (waiting for room if landed chunks have not
+ * freed enough yet).  Returns with a ticket; the arrival time is the moment
+ * of the call.  Needs ntimes % 16 == 0. */
 BF_API int bf_server_submit(bf_server *server, int channel, int nchannels, int64_t ntimes, const uint8_t *E,
                             int e_on_device, uint8_t *J, int j_on_device, int64_t *ticket);
 
