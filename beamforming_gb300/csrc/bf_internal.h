@@ -34,6 +34,18 @@ __device__ __forceinline__ int a2_nibble(const uint8_t *A, int64_t i) {
                  : static_cast<int>(static_cast<int8_t>(static_cast<uint8_t>(x << 4))) >> 4;
 }
 
+// max(-7, min(7, int(lrint(x)))) of cpu.cxx:38-39 for any float x.  lrint
+// rounds half to even to a 64-bit long and the int(...) narrowing comes before
+// the clamp, so 2^31 <= |x| < 2^63 keeps the low 32 bits of the rounded value
+// (two's complement); NaN, infinities and |x| >= 2^63 give 0, the x86-64
+// lrint result LONG_MIN narrowed (the reference's own build, checked against
+// it on huge gains).
+__device__ __forceinline__ int requant_narrow(float x) {
+  if (!(fabsf(x) < 9.223372036854775808e18f)) return 0;  // 2^63
+  const int v = static_cast<int>(static_cast<unsigned>(static_cast<unsigned long long>(__float2ll_rn(x))));
+  return max(-7, min(7, v));
+}
+
 // Real and imaginary part of the weight of dish d, beam b, frequency f.
 __device__ __forceinline__ void load_a(const uint8_t *A, int a_layout, int64_t f, int64_t b, int64_t d, int64_t B,
                                        int64_t D, int &re, int &im) {
@@ -70,17 +82,20 @@ struct TcWeights {
   uint8_t *W = nullptr;      // [F][nw][2D]
   uint8_t *dig = nullptr;    // [F][nw_pad][kDigitRow]
   float *gs = nullptr;       // [F][nw_pad / 2]: 512 * G, zero past B (the epilogue's gains)
+  int *gwide = nullptr;      // [F]: nonzero when a gain of the frequency can take |G * raw| to 2^31
   const float *G = nullptr;  // [F][B] (device; read by the weight preparation)
 };
 
-// The digit rows and the scaled gains share one allocation: digit rows first
-// (F * nw_pad * 32 bytes, a multiple of 32), then the gains.
+// The digit rows, the scaled gains and the wide-gain flags share one
+// allocation: digit rows first (F * nw_pad * 32 bytes, a multiple of 32), then
+// the gains (F * nw_pad / 2 floats), then one int per frequency.
 inline size_t tc_extra_bytes(const TcWeights &w) {
-  return static_cast<size_t>(w.F) * w.nw_pad * (kDigitRow + sizeof(float) / 2);
+  return static_cast<size_t>(w.F) * w.nw_pad * (kDigitRow + sizeof(float) / 2) + static_cast<size_t>(w.F) * sizeof(int);
 }
 inline void tc_set_extra(TcWeights &w, uint8_t *p) {
   w.dig = p;
   w.gs = reinterpret_cast<float *>(p + static_cast<size_t>(w.F) * w.nw_pad * kDigitRow);
+  w.gwide = reinterpret_cast<int *>(w.gs + static_cast<size_t>(w.F) * w.nw_pad / 2);
 }
 
 // True when the tensor-core kernel handles this shape.
@@ -124,6 +139,7 @@ struct TcProblem {  // 128-byte aligned through its tensor maps
   const uint8_t *jbase;        // start of the whole J buffer: byte positions of the fused adler32
   unsigned long long *adler;   // null, or the fused adler32 sums {sum d_i, sum i * d_i} (device)
   const float *gs;   // scaled gains [F][npass * nb_pass]
+  const int *gwide;  // [F]: the frequency needs the narrowing requantisation (huge or non-finite gains)
   int64_t jpitch;    // bytes between consecutive (b, f, p) rows of J (J2: (b, f) rows are 2 * jpitch apart)
   int jlayout;       // JLayout
   int T, F, B;

@@ -13,7 +13,8 @@
 //   g_noalloc_scratch   kNoAllocScratchBytes = 4 MiB, 256-byte aligned
 //     [0, 256)                    device error word (cleared every call)
 //     [256, 256 + extra bytes)    dig[f][n][32] E4M3, F * npass * 2 * nb_pass * 32, then
-//                                 512 * G[f][b] floats, F * npass * nb_pass
+//                                 512 * G[f][b] floats, F * npass * nb_pass, then
+//                                 one wide-gain flag (int) per frequency
 //     [.., .. + W bytes)          W[f][n][k]   E4M3,  F * 2 * roundup(B, 8) * 2 * D
 //
 // Every GPU that loads the library holds these 4 MiB until the process exits.

@@ -99,6 +99,18 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int *er
   }
 }
 
+// Bounded wait for the error path, which ignores the error word: a role that
+// gives up waits with it for the copies it already issued to land before the
+// CTA exits (at most kWaitTimeoutNs per barrier).
+__device__ __forceinline__ bool mbar_wait_drain(uint32_t bar, uint32_t parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = globaltimer_ns();
+  for (uint32_t i = 1;; ++i) {
+    if (mbar_try_wait_sleep(bar, parity, 200000u)) return true;
+    if (i % kPollCheck == 0 && globaltimer_ns() - t0 > kWaitTimeoutNs) return false;
+  }
+}
+
 // ---------------------------------------------------------------- proxies
 __device__ __forceinline__ void fence_proxy_async_smem() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");

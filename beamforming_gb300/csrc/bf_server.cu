@@ -92,14 +92,20 @@ class Pool {
 };
 
 // Host memory the copy engines read and write asynchronously (pinned or
-// registered); pageable memory answers cudaMemoryTypeUnregistered.
-bool pinned_host(const void *p) {
+// registered); pageable memory answers cudaMemoryTypeUnregistered.  Both the
+// first and the last byte of the buffer are checked, so a buffer registered
+// only in part goes through the staging ring (a buffer registered in several
+// pieces must have no pageable gap between them).
+bool pinned_byte(const void *p) {
   cudaPointerAttributes at{};
   if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
     (void)cudaGetLastError();
     return false;
   }
   return at.type == cudaMemoryTypeHost;
+}
+bool pinned_host(const void *p, size_t bytes) {
+  return pinned_byte(p) && (bytes <= 1 || pinned_byte(static_cast<const uint8_t *>(p) + (bytes - 1)));
 }
 
 struct Request {
@@ -174,7 +180,8 @@ struct bf_server {
 
   void run();
   bool launch(Flight &fl, const std::vector<Request> &reqs, int *ntiles);
-  void finish_locked(Flight &fl);
+  void retire_locked(Flight &fl, std::vector<Request> &staged);
+  void hand_out(std::unique_lock<std::mutex> &lk, std::vector<Request> &staged);
 };
 
 namespace {
@@ -187,6 +194,7 @@ TcWeights channel_view(const TcWeights &w, int c0, int n) {
   v.W = w.W + static_cast<int64_t>(c0) * w.nw * 2 * w.D;
   v.dig = w.dig + static_cast<int64_t>(c0) * w.nw_pad * kDigitRow;
   v.gs = w.gs + static_cast<int64_t>(c0) * (w.nw_pad / 2);
+  v.gwide = w.gwide + c0;
   v.G = w.G + static_cast<int64_t>(c0) * w.B;
   return v;
 }
@@ -246,25 +254,50 @@ bool bf_server::launch(Flight &fl, const std::vector<Request> &reqs, int *ntiles
   return true;
 }
 
-void bf_server::finish_locked(Flight &fl) {
+// Retires a landed launch (mutex held): frees its pool memory, its slot and
+// its weight-version references, and completes its chunks.  A chunk whose J
+// still sits in the staging ring is moved to `staged` instead and completes
+// in hand_out(), which copies it to the caller without the mutex.
+void bf_server::retire_locked(Flight &fl, std::vector<Request> &staged) {
   if (*fl.err_host != 0 && status == BF_OK) status = BF_ERR_DEVICE_TIMEOUT;  // a kernel wait gave up
   for (Request &r : fl.reqs) {
     --ver[r.version].refs;
     if (!r.e_on_device) pool.release(r.dE, r.e_bytes);
     if (!r.j_on_device) pool.release(r.dJ, r.j_bytes);
-    Clock::time_point landed = fl.landed_at;
-    if (r.sJ) {  // the chunk's J is in the ring: hand it to the caller's buffer
-      std::memcpy(r.J_user, r.sJ, r.j_bytes);
-      staging.release(r.sJ, r.j_bytes);
-      landed = Clock::now();
-    }
     if (r.sE) staging.release(r.sE, r.e_bytes);
-    done_latency[r.ticket] = std::chrono::duration<double>(landed - r.arrival).count();
+    r.sE = nullptr;
+    if (r.sJ) {
+      staged.push_back(r);
+      continue;
+    }
+    done_latency[r.ticket] = std::chrono::duration<double>(fl.landed_at - r.arrival).count();
     ++completed;
   }
   fl.reqs.clear();
   fl.busy = false;
   fl.landed = false;
+  cv_done.notify_all();
+}
+
+// Copies the J of staged chunks from the ring into the callers' buffers with
+// the mutex released (a chunk's J can be hundreds of MB), then frees their
+// ring room and completes them.  Called with `lk` held; returns with it held.
+void bf_server::hand_out(std::unique_lock<std::mutex> &lk, std::vector<Request> &staged) {
+  if (staged.empty()) return;
+  lk.unlock();
+  std::vector<Clock::time_point> done(staged.size());
+  for (size_t i = 0; i < staged.size(); ++i) {
+    std::memcpy(staged[i].J_user, staged[i].sJ, staged[i].j_bytes);
+    done[i] = Clock::now();
+  }
+  lk.lock();
+  for (size_t i = 0; i < staged.size(); ++i) {
+    const Request &r = staged[i];
+    staging.release(r.sJ, r.j_bytes);
+    done_latency[r.ticket] = std::chrono::duration<double>(done[i] - r.arrival).count();
+    ++completed;
+  }
+  staged.clear();
   cv_done.notify_all();
 }
 
@@ -303,9 +336,11 @@ void bf_server::run() {
       }
     }
     lk.lock();
-    // retire landed launches: their pool memory and slot become free
+    // retire landed launches: their pool memory and slot become free; J that
+    // waits in the staging ring is handed out after the next launch is queued
+    std::vector<Request> staged;
     for (auto &fp : flights)
-      if (fp->busy && fp->landed) finish_locked(*fp);
+      if (fp->busy && fp->landed) retire_locked(*fp, staged);
     // admit queued chunks into a free slot while the pool has room for them
     Flight *slot = nullptr;
     for (auto &fp : flights)
@@ -343,10 +378,12 @@ void bf_server::run() {
         stats.chunks_launched += n;
         stats.max_batch_seen = std::max<int64_t>(stats.max_batch_seen, n);
         if (!ok && status == BF_OK) status = BF_ERR_CUDA;
+        hand_out(lk, staged);
         lk.unlock();
         continue;
       }
     }
+    hand_out(lk, staged);
     bool inflight = false;
     for (auto &fp : flights) inflight |= fp->busy;
     if (stop.load() && ((queue.empty() && !inflight) || status != BF_OK)) break;
@@ -438,8 +475,8 @@ int bf_server_submit(bf_server *s, int channel, int nchannels, int64_t ntimes, c
   // room is taken here, waiting for landed chunks to free it if need be, and
   // E is copied in by this thread, so the server's device copies stay
   // asynchronous; J is copied out of the ring when the chunk lands
-  const bool stage_e = !r.e_on_device && !pinned_host(E);
-  const bool stage_j = !r.j_on_device && !pinned_host(J);
+  const bool stage_e = !r.e_on_device && !pinned_host(E, r.e_bytes);
+  const bool stage_j = !r.j_on_device && !pinned_host(J, r.j_bytes);
   const size_t need = (stage_e ? r.e_bytes + 256 : 0) + (stage_j ? r.j_bytes + 256 : 0);
   if (need > 0 && need <= s->staging.size()) {
     std::unique_lock<std::mutex> lk(s->mu);

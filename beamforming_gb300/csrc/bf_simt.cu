@@ -24,11 +24,11 @@ __device__ __forceinline__ uint32_t pack4(int a, int b, int c, int d) {
   return (static_cast<uint32_t>(a) & 0xFFu) | ((static_cast<uint32_t>(b) & 0xFFu) << 8) |
          ((static_cast<uint32_t>(c) & 0xFFu) << 16) | ((static_cast<uint32_t>(d) & 0xFFu) << 24);
 }
-// clamp(lrint(G * float(raw)), -7, 7): cpu.cxx:37-39.  __fmul_rn is one IEEE
-// single multiply (never fused); __float2int_rn rounds half to even like lrint.
+// clamp(int(lrint(G * float(raw))), -7, 7): cpu.cxx:37-39.  __fmul_rn is one
+// IEEE single multiply (never fused); requant_narrow rounds and narrows like
+// int(lrint(x)).
 __device__ __forceinline__ int requant(float g, int raw) {
-  const int r = __float2int_rn(__fmul_rn(g, __int2float_rn(raw)));
-  return max(-7, min(7, r));
+  return requant_narrow(__fmul_rn(g, __int2float_rn(raw)));
 }
 
 __global__ void __launch_bounds__(kThreads) bf_form_beams_simt(uint8_t *__restrict__ J, const uint8_t *__restrict__ E,

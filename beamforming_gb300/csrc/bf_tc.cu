@@ -376,7 +376,7 @@ __global__ void __launch_bounds__(Roles<kEpiW>::kThreads, 1) bf_form_beams_tc(co
       }
       if (!ok) {  // let copies already issued land before the CTA exits
         for (uint32_t k = (issued >= static_cast<uint32_t>(R) ? issued - R : 0); k < issued; ++k)
-          mbar_wait(raw_full(static_cast<int>(k % R)), (k / R) & 1u, err, kDevTimeoutFull);
+          mbar_wait_drain(raw_full(static_cast<int>(k % R)), (k / R) & 1u);
       }
     }
   } else if (warp == kWProdWarp) {
@@ -429,9 +429,9 @@ __global__ void __launch_bounds__(Roles<kEpiW>::kThreads, 1) bf_form_beams_tc(co
       }
       if (!ok) {
         for (uint32_t k = (it >= static_cast<uint32_t>(SW) ? it - SW : 0); k < it; ++k)
-          mbar_wait(w_full(static_cast<int>(k % SW)), (k / SW) & 1u, err, kDevTimeoutFull);
+          mbar_wait_drain(w_full(static_cast<int>(k % SW)), (k / SW) & 1u);
         for (uint32_t k = (dit >= static_cast<uint32_t>(kDigSlots) ? dit - kDigSlots : 0); k < dit; ++k)
-          mbar_wait(d_full(static_cast<int>(k % kDigSlots)), (k / kDigSlots) & 1u, err, kDevTimeoutFull);
+          mbar_wait_drain(d_full(static_cast<int>(k % kDigSlots)), (k / kDigSlots) & 1u);
       }
     }
   } else if (warp == kMmaWarp) {
@@ -599,6 +599,9 @@ __global__ void __launch_bounds__(Roles<kEpiW>::kThreads, 1) bf_form_beams_tc(co
       // exactly and the power-of-two scaling is exact, so (512 G) * (raw / 512)
       // rounds like G * raw (cpu.cxx:37)
       const float *gcur = P.gs + static_cast<int64_t>(f) * P.npass * P.nb_pass + b0;
+      // huge or non-finite gains of this frequency: requantise with the
+      // narrowing of cpu.cxx:38 (tile-uniform branch, normally not taken)
+      const bool wide = __ldg(P.gwide + f) != 0;
       if (!__all_sync(0xffffffffu, mbar_wait(accfull(ab), aph, err, kDevTimeoutAccFull))) break;
       tc_fence_after();
       const uint32_t acc_addr = tmem_base + ab * kAccCols + lane_addr;
@@ -644,10 +647,18 @@ __global__ void __launch_bounds__(Roles<kEpiW>::kThreads, 1) bf_form_beams_tc(co
         // multiply, the lower clamp (to -7.25: same result after rounding), a
         // round-half-even conversion, and the upper clamp by the saturating pack
         int qre[8], qim[8];
+        if (!wide) {
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          qre[i] = __float2int_rn(fmaxf(__fmul_rn(gv[i], __uint_as_float(r[i])), -7.25f));
-          qim[i] = __float2int_rn(fmaxf(__fmul_rn(gv[i], __uint_as_float(r[8 + i])), -7.25f));
+          for (int i = 0; i < 8; ++i) {
+            qre[i] = __float2int_rn(fmaxf(__fmul_rn(gv[i], __uint_as_float(r[i])), -7.25f));
+            qim[i] = __float2int_rn(fmaxf(__fmul_rn(gv[i], __uint_as_float(r[8 + i])), -7.25f));
+          }
+        } else {
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            qre[i] = requant_narrow(__fmul_rn(gv[i], __uint_as_float(r[i])));
+            qim[i] = requant_narrow(__fmul_rn(gv[i], __uint_as_float(r[8 + i])));
+          }
         }
         // ucomplex4 bytes of beams 0-3 and 4-7 for this lane's time
         uint32_t w[2];
@@ -738,7 +749,8 @@ __global__ void __launch_bounds__(32 * kPrepRows) bf_prep_weights(const uint8_t 
                                                                    uint8_t *__restrict__ W,
                                                                    uint8_t *__restrict__ dig,
                                                                    const float *__restrict__ G, float *__restrict__ gs,
-                                                                   int B, int D, int nw, int nw_pad, int a_layout) {
+                                                                   int *__restrict__ gwide, int B, int D, int nw,
+                                                                   int nw_pad, int a_layout) {
   // E4M3 codes of the integers 0..8
   const uint8_t e4m3_pos[9] = {0x00, 0x38, 0x40, 0x44, 0x48, 0x4A, 0x4C, 0x4E, 0x50};
   const int rblocks = (nw_pad + kPrepRows - 1) / kPrepRows;  // blocks per frequency
@@ -747,8 +759,18 @@ __global__ void __launch_bounds__(32 * kPrepRows) bf_prep_weights(const uint8_t 
   const int lane = threadIdx.x & 31;
   if (static_cast<int>(blockIdx.x) % rblocks == 0) {  // the frequency's scaled gains: 512 G, zero past B
     const int ng = nw_pad / 2;
-    for (int i = threadIdx.x; i < ng; i += blockDim.x)
-      gs[static_cast<int64_t>(f) * ng + i] = i < B ? 512.0f * G[static_cast<int64_t>(f) * B + i] : 0.0f;
+    // |raw| <= 128 D, so with |G| * 128 D < 2^30 every product G * raw stays
+    // below 2^31 and the plain requantisation is exact; otherwise (or for a
+    // non-finite gain) the frequency takes the narrowing one of cpu.cxx:38
+    const float wide_at = 1073741824.0f / (128.0f * static_cast<float>(D));
+    int wide = 0;
+    for (int i = threadIdx.x; i < ng; i += blockDim.x) {
+      const float g = i < B ? G[static_cast<int64_t>(f) * B + i] : 0.0f;
+      gs[static_cast<int64_t>(f) * ng + i] = 512.0f * g;
+      wide |= !(fabsf(g) < wide_at);
+    }
+    wide = __syncthreads_or(wide);
+    if (threadIdx.x == 0) gwide[f] = wide;
   }
   if (n >= nw_pad) return;  // the whole warp
   int sum = 0;
@@ -875,7 +897,7 @@ cudaError_t launch_prep_weights(const TcWeights &w, const uint8_t *A, cudaStream
   const int64_t blocks = static_cast<int64_t>((w.nw_pad + kPrepRows - 1) / kPrepRows) * w.F;
   if (blocks > 0x7FFFFFFF) return cudaErrorInvalidValue;
   bf_prep_weights<<<static_cast<unsigned>(blocks), 32 * kPrepRows, 0, s>>>(
-      A, w.W, w.dig, w.G, w.gs, static_cast<int>(w.B), static_cast<int>(w.D), w.nw, w.nw_pad, a_layout);
+      A, w.W, w.dig, w.G, w.gs, w.gwide, static_cast<int>(w.B), static_cast<int>(w.D), w.nw, w.nw_pad, a_layout);
   return cudaGetLastError();
 }
 
@@ -900,6 +922,7 @@ static cudaError_t make_problem(TcProblem &P, const TcWeights &w, int64_t T, uin
   P.ntt = static_cast<int>((T + kTT - 1) / kTT);
   P.nw_pad = w.nw_pad;
   P.gs = w.gs;
+  P.gwide = w.gwide;
   {  // E[t][f][d*p] bytes: dims {2D, F, T}
     const cuuint64_t dims[3] = {static_cast<cuuint64_t>(2 * D), static_cast<cuuint64_t>(F),
                                 static_cast<cuuint64_t>(T)};

@@ -44,7 +44,8 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU-baseline sample")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0,
+                    help="target length of the CPU-baseline sample (the whole chunk when it fits)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument(
@@ -178,17 +179,37 @@ class ClockSampler:
         }
 
 
-def cpu_baseline(target_s: float):
-    """The oracle (the reference's cpu.cxx restated) on a sample of frequencies of the workload."""
-    import beamforming_gb300 as bf
+def oracle_inputs(O, d):
+    """The workload's seeded E, A and G from the oracle's own generator (the
+    same bytes as the library's; see the oracle's bfo_fill_random)."""
+    od = O.Dims(d.ntimes, d.nfrequencies, d.ndishes, d.npolarizations, d.nbeams)
+    return od, *O.seeded_inputs(od, WORKLOAD["seed"])
+
+
+def golden_full_adler32():
+    """adler32 of J that the reference's own cpu.cxx gave on the full chunk
+    (tests/golden/golden.json, made by tests/golden/make_golden.py), or None."""
+    path = os.path.join(ROOT, "tests", "golden", "golden.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as fp:
+        g = json.load(fp)
+    key = tuple(WORKLOAD[k] for k in ("ntimes", "nfrequencies", "ndishes", "npolarizations", "nbeams", "seed"))
+    for rec in g.get("full", []):
+        if (rec["T"], rec["F"], rec["D"], rec["P"], rec["B"], rec["seed"]) == key:
+            return int(rec["adler32"])
+    return None
+
+
+def cpu_baseline(target_s: float, gpu_adler32: int):
+    """The oracle (the reference's cpu.cxx restated) on the workload, timed on
+    the host cores.  When the whole chunk fits the time target it runs all of
+    it and its J must give the GPU's adler32; otherwise it runs a prefix of
+    the frequencies, checked byte for byte against the GPU's J there."""
     from oracle import oracle as O
 
     d = dims()
-    E = np.empty(d.esize, np.uint8)
-    bf.fill_random_host(E, WORKLOAD["seed"], 0)
-    A = np.empty(d.asize, np.uint8)
-    bf.fill_random_host(A, WORKLOAD["seed"], 1)
-    G = bf.gains(d)
+    od, E, A, G = oracle_inputs(O, d)
     E4 = E.reshape(d.ntimes, d.nfrequencies, -1)
     A2 = A.reshape(d.nfrequencies, -1)
     G2 = G.reshape(d.nfrequencies, -1)
@@ -199,12 +220,17 @@ def cpu_baseline(target_s: float):
         As = np.ascontiguousarray(A2[:nf]).reshape(-1)
         Gs = np.ascontiguousarray(G2[:nf]).reshape(-1)
         t0 = time.perf_counter()
-        O.form_beams(sub, Es, As, Gs)
-        return time.perf_counter() - t0, sub.cmacs
+        J = O.form_beams(sub, Es, As, Gs)
+        return time.perf_counter() - t0, sub.cmacs, J
 
-    t1, _ = run(1)
+    t1, _, _ = run(1)
     nf = int(max(1, min(d.nfrequencies, round(target_s / max(t1, 1e-3)))))
-    t, cm = run(nf)
+    t, cm, J = run(nf)
+    if nf == d.nfrequencies:
+        parity = O.adler32(J) == gpu_adler32
+        check = f"adler32 of the oracle's J over all frequencies = 0x{O.adler32(J):08x} (GPU 0x{gpu_adler32:08x})"
+    else:
+        parity, check = None, f"{nf} of {d.nfrequencies} frequencies: no whole-J checksum"
     cores = os.cpu_count() or 1
     return {
         "value": cm / t,
@@ -213,39 +239,63 @@ def cpu_baseline(target_s: float):
         "kind": "port",
         "sample": f"{nf} of {d.nfrequencies} frequencies of the workload ({cm:.3e} CMAC, {t:.2f} s, "
         f"OpenMP threads = {cores})",
+        "parity": parity,
+        "parity_check": check,
     }
 
 
+# The whole reference arm stays within about this many seconds of CPU work.
+REFERENCE_BUDGET_S = 150.0
+
+
 def run_reference(args):
-    """Reference arm: the reference's CPU algorithm on the host cores."""
+    """Reference arm: the reference's CPU algorithm on the host cores.  The
+    reference's own cpu.cxx is x86 code compiled from sources that are not on
+    the GPU host, so this times its restatement, the oracle (cpu.cxx:15-46,
+    OpenMP over every host thread), on the same seeded chunk as the GPU arm.
+    Each step is one pass over the whole chunk (all frequencies) when
+    warmup + steps such passes fit REFERENCE_BUDGET_S; otherwise each step
+    takes the same prefix of the frequencies, sized to fit.  Nothing of the
+    GPU library is loaded."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    import beamforming_gb300 as bf  # noqa: F401  (workload generator)
     from oracle import oracle as O
 
     d = dims()
-    nf = 1  # one frequency of the chunk per step
-    sub = O.Dims(d.ntimes, nf, d.ndishes, 2, d.nbeams)
-    E = np.empty(d.esize, np.uint8)
-    bf.fill_random_host(E, WORKLOAD["seed"], 0)
-    A = np.empty(d.asize, np.uint8)
-    bf.fill_random_host(A, WORKLOAD["seed"], 1)
-    G = bf.gains(d)
+    od, E, A, G = oracle_inputs(O, d)
     E4 = E.reshape(d.ntimes, d.nfrequencies, -1)
+    A2 = A.reshape(d.nfrequencies, -1)
+    G2 = G.reshape(d.nfrequencies, -1)
+
+    def sample(nf):
+        sub = O.Dims(d.ntimes, nf, d.ndishes, 2, d.nbeams)
+        if nf == d.nfrequencies:
+            return sub, E, A, G
+        return (sub, np.ascontiguousarray(E4[:, :nf]).reshape(-1), np.ascontiguousarray(A2[:nf]).reshape(-1),
+                np.ascontiguousarray(G2[:nf]).reshape(-1))
+
+    # the first warm-up pass (whole chunk) sizes the per-step sample
+    t0 = time.perf_counter()
+    J = O.form_beams(od, E, A, G)
+    t_full = time.perf_counter() - t0
+    whole = O.adler32(J)
+    ref = golden_full_adler32()
+    nsteps = max(1, args.warmup) + args.steps
+    nf = d.nfrequencies
+    if nsteps * t_full > REFERENCE_BUDGET_S:
+        nf = max(1, int(d.nfrequencies * REFERENCE_BUDGET_S / (nsteps * t_full)))
+    sub, Es, As, Gs = sample(nf)
     samples = []
-    for i in range(args.warmup + args.steps):
-        f = i % d.nfrequencies
-        Es = np.ascontiguousarray(E4[:, f]).reshape(-1)
-        As = np.ascontiguousarray(A.reshape(d.nfrequencies, -1)[f])
-        Gs = np.ascontiguousarray(G.reshape(d.nfrequencies, -1)[f])
+    for i in range(max(1, args.warmup) - 1 + args.steps):
         t0 = time.perf_counter()
         O.form_beams(sub, Es, As, Gs)
-        if i >= args.warmup:
+        if i >= max(1, args.warmup) - 1:
             samples.append(time.perf_counter() - t0)
     total = sum(samples)
     value = sub.cmacs * len(samples) / total
     cores = os.cpu_count() or 1
+    what = "the whole chunk (all 84 frequencies)" if nf == d.nfrequencies else f"{nf} of {d.nfrequencies} frequencies"
     line = {
         "impl": "reference",
         "metric": METRIC,
@@ -259,16 +309,19 @@ def run_reference(args):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "int4 complex in, int32 sums",
-        "data": "synthetic (seeded uniform 4-bit complex)",
-        "config": {"workload": WORKLOAD_NAME, **WORKLOAD, "sample_per_step": "one frequency (t=32768, d=512, b=96)"},
+        "data": "synthetic (seeded uniform 4-bit complex; G from the reference setup() formula)",
+        "config": {"workload": WORKLOAD_NAME, **WORKLOAD, "sample_per_step": what},
         "cpu_baseline": {
             "value": value,
             "unit": UNIT,
             "cores": cores,
             "kind": "port",
-            "sample": "one frequency of the chunk per step; oracle restatement of cpu.cxx:15-46 with OpenMP",
+            "sample": f"{what} per step; oracle restatement of cpu.cxx:15-46, OpenMP threads = {cores}",
         },
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "adler32_J": f"0x{whole:08x}",
+        "parity": {"reference_cpu_cxx_adler32": None if ref is None else f"0x{ref:08x}",
+                   "equal": None if ref is None else whole == ref},
     }
     print(json.dumps(line), flush=True)
 
@@ -371,7 +424,6 @@ def run_ours(args):
     ev1.record(stream)
     barrier()
     ms = ev0.elapsed_time(ev1) / args.steps
-    clk = clocks.stop() if rank == 0 else None
     bf.stream_status(stream)
     ms_max = max_over_ranks(ms, dist, "cuda")
     value = job_value(d.cmacs, world, ms_max)
@@ -390,11 +442,30 @@ def run_ours(args):
     torch.cuda.synchronize()
     bf.stream_status(stream)
     k_ms = statistics.mean(a.elapsed_time(b) for a, b in evs)
+    # the weight preparation of every form_beams_ex call (A -> operand W,
+    # digit rows, scaled gains), timed alone: update() on the resident weights
+    pevs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(20)]
+    for a, b in pevs:
+        a.record(stream)
+        W.update(A, G, stream=stream)
+        b.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop() if rank == 0 else None
+    p_ms = statistics.mean(a.elapsed_time(b) for a, b in pevs)
     assert bf.adler32_device(J) == checksum
     W.close()
     alg_bytes = d.esize + d.jsize + d.asize + 4 * d.gsize
     roofline = roofline_of(bf, stream, d.cmacs, alg_bytes, k_ms, "bf_form_beams_tc")
     roofline["traffic"] = profile_traffic()
+    # clock-normalised kernel time, comparable across runs whose power-capped
+    # SM clock differs: kernel ms x median SM MHz of this run = kilocycles
+    if clk and clk.get("sm_mhz"):
+        roofline["kernel_kcycles_at_median_clock"] = round(k_ms * clk["sm_mhz"], 1)
+    step_split = {"step_ms": round(ms_max, 4), "kernel_ms": round(k_ms, 4),
+                  "weights_prep_ms": round(p_ms, 4),
+                  "rest_ms": round(ms_max - k_ms - p_ms, 4),
+                  "note": "step = bf_form_beams_ex (weights prepared every call) back to back; kernel = resident "
+                          "launches with events around each; prep = bf_weights_update (A, G copies + preparation)"}
 
     # the checksum the reference prints after form_beams (arraysizes.cxx:79):
     # summed in the kernel's epilogue vs a second pass over J; both calls are
@@ -438,7 +509,7 @@ def run_ours(args):
         "api": "bf_form_beams_adler vs bf_form_beams_ex + bf_adler32_device, device buffers; host wall and CUDA events",
     }
 
-    e2e = None
+    e2e = e2e_pageable = None
     if not args.no_e2e:
         Eh = torch.empty(d.esize, dtype=torch.uint8, pin_memory=True)
         Ah = torch.empty(d.asize, dtype=torch.uint8, pin_memory=True)
@@ -467,10 +538,36 @@ def run_ours(args):
             "d2h_bytes_per_step": d.jsize,
             "api": "bf_form_beams_ex(ptr_kind=BF_PTR_HOST), pinned host buffers",
         }
+        del Eh, Ah, Gh, Jh, En, An, Gn, Jn
+        # the drop-in case proper: the reference's main passes std::vector
+        # storage (cpu.cxx:48-67), i.e. pageable host memory
+        Ep = E.cpu().numpy().copy()
+        Ap, Gp = A.cpu().numpy().copy(), G.cpu().numpy().copy()
+        Jp = np.empty(d.jsize, np.uint8)
+        bf.form_beams_ex(d, Jp, Ep, Ap, Gp)
+        n_p = max(3, min(args.steps, 10))
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(n_p):
+            bf.form_beams_ex(d, Jp, Ep, Ap, Gp)
+        barrier()
+        p_s = (time.perf_counter() - t0) / n_p
+        assert zlib.adler32(Jp.tobytes()) == checksum
+        e2e_pageable = {
+            "value": d.cmacs * world / p_s,
+            "unit": UNIT,
+            "ms_per_step": round(1e3 * p_s, 3),
+            "h2d_bytes_per_step": d.esize + d.asize + 4 * d.gsize,
+            "d2h_bytes_per_step": d.jsize,
+            "api": "form_beams path bf_form_beams_ex(ptr_kind=BF_PTR_HOST), pageable host buffers (numpy)",
+        }
+        del Ep, Ap, Gp, Jp
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(args.cpu_seconds)
+        cpu = cpu_baseline(args.cpu_seconds, checksum)
+        assert cpu["parity"] in (True, None), cpu["parity_check"]
+    ref_adler = golden_full_adler32()
 
     if rank == 0:
         line = {
@@ -493,9 +590,15 @@ def run_ours(args):
                 "l2": "inputs larger than L2 (E = 2.82 GB), no flush",
                 "adler32_J": f"0x{checksum:08x}",
             },
+            "parity": {"adler32_J": f"0x{checksum:08x}",
+                       "reference_cpu_cxx_adler32": None if ref_adler is None else f"0x{ref_adler:08x}",
+                       "equal_to_reference": None if ref_adler is None else checksum == ref_adler,
+                       "oracle_whole_chunk": None if cpu is None else cpu["parity"]},
             "roofline": roofline,
+            "step_split": step_split,
             "cpu_baseline": cpu,
             "e2e": e2e,
+            "e2e_pageable": e2e_pageable,
             "checksum": checksum_block,
             "clocks": clk,
             "gpu_launches": 2 * args.steps,

@@ -3,9 +3,15 @@
  *
  * Computes, for every beam b, frequency f, polarization p and time t,
  *
- *   J[b][f][p][t] = ucomplex4(clamp(lrint(G[f][b] * float(re)), -7, 7),
- *                             clamp(lrint(G[f][b] * float(im)), -7, 7))
+ *   J[b][f][p][t] = ucomplex4(clamp(int(lrint(G[f][b] * float(re))), -7, 7),
+ *                             clamp(int(lrint(G[f][b] * float(im))), -7, 7))
  *   re + i*im    = sum_d A[f][b][d] * E[t][f][d][p]        (exact integers)
+ *
+ * As in cpu.cxx:38, lrint's 64-bit result is narrowed to int before the
+ * clamp: a product with 2^31 <= |G * raw| < 2^63 keeps its low 32 bits (so it
+ * clamps to 0, +7 or -7 by those bits), and a NaN, infinite or |G * raw| >= 2^63
+ * product gives 0 (what the reference's x86-64 build returns).  Any float G is
+ * accepted.
  *
  * over 4-bit complex data stored as ucomplex4 bytes (real part in the high
  * nibble, imaginary part in the low nibble, each stored as value + 8).  The
@@ -284,7 +290,7 @@ BF_API int bf_server_destroy(bf_server *server);
  * E, A, G and J are device pointers.  Limits: the tensor-core shape rules
  * (npolarizations == 2, ndishes % 8 == 0, ntimes % 16 == 0, E and J 16-byte
  * aligned, ndishes <= 2048; else BF_ERR_UNSUPPORTED) and
- *   256 + roundup256(68 * F * npass * nb) + F * 2 * roundup(B, 8) * 2 * D <= 4 MiB
+ *   256 + roundup256(68 * F * npass * nb + 4 * F) + F * 2 * roundup(B, 8) * 2 * D <= 4 MiB
  * (npass = ceil(roundup(B, 8) / 96), nb = roundup(ceil(roundup(B, 8) / npass), 8); else
  * BF_ERR_TOO_LARGE) -- e.g. f=16, b=96, d=512 fits, f=84 does not.
  * Synchronous: returns once the pass on `stream` has finished, with its status.

@@ -11,10 +11,12 @@
 # oracle/_ref/ (git-ignored).
 #
 # usage: oracle/build_ref.sh [REFERENCE_DIR]
+#   REFERENCE_DIR defaults to $BF_REFERENCE_DIR, else the checkout this
+#   recipe was written against (/root/reference).
 #   builds   oracle/_ref/<T>_<F>_<D>_<P>_<B>/cpu     (stock program, prints checksum)
 #            oracle/_ref/<T>_<F>_<D>_<P>_<B>/ref_io  (reads E/A/G files, writes J)
 set -euo pipefail
-REF=${1:-/root/reference}
+REF=${1:-${BF_REFERENCE_DIR:-/root/reference}}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 if [ ! -f "$REF/cpu.cxx" ]; then
@@ -30,7 +32,9 @@ CFLAGS="-std=c11 -fopenmp $ARCHFLAG -O3 -DNDEBUG"
 CXXFLAGS="-std=c++17 -fopenmp -Drestrict=__restrict__ $ARCHFLAG -O3 -DNDEBUG"
 
 # Shapes T F D P B: the golden-checksum shapes of arraysizes.cxx:54-59, the
-# plain-beamform workload, and small ragged shapes for byte comparison.
+# plain-beamform workload, the full single-GPU chunk (t=32768 f=84), the
+# wide-array shape (d=1024 b=512), the deepest dish count the tensor-core
+# path accepts (d=2048), and small ragged shapes for byte comparison.
 SHAPES=${BF_REF_SHAPES:-"
 32768 16 512 2 96
 32768 32 512 2 96
@@ -48,6 +52,9 @@ SHAPES=${BF_REF_SHAPES:-"
 16 2 32 1 8
 256 1 512 2 128
 128 2 1024 2 512
+32768 84 512 2 96
+16384 16 1024 2 512
+64 2 2048 2 96
 "}
 
 build_one() {

@@ -31,13 +31,20 @@ int bfo_decode_im(uint8_t data) { return (int)(int8_t)(uint8_t)((uint8_t)(data ^
 /* Requantisation of one accumulator: cpu.cxx:37-39.
  *   max(-7, min(7, int(lrint(G * float(raw)))))
  * G * float(raw) is one IEEE single-precision multiply; lrint rounds half to
- * even in the default rounding mode. */
+ * even in the default rounding mode and returns a 64-bit long.  The int(...)
+ * narrowing comes BEFORE the clamp, so a product with 2^31 <= |x| < 2^63 keeps
+ * only its low 32 bits (two's complement, as GCC defines the conversion): the
+ * clamp then gives 0, +7 or -7 from those bits, not the sign of x.  For NaN,
+ * infinities and |x| >= 2^63 lrint has no long to return; the reference's
+ * x86-64 build returns LONG_MIN (the "integer indefinite" of cvtss2si), whose
+ * low 32 bits are 0.  Both rules are written out here instead of relying on
+ * the host's lrintf, so the oracle gives the same bytes on every host. */
 static inline int requant(float g, int32_t raw) {
   const float x = g * (float)raw;
-  long r = lrintf(x);
-  if (r > 7) r = 7;
-  if (r < -7) r = -7;
-  return (int)r;
+  if (!(fabsf(x) < 0x1p63f)) return 0; /* NaN, +-inf, |x| >= 2^63 */
+  const uint32_t lo = (uint32_t)(uint64_t)(int64_t)lrintf(x); /* exact below 2^63 */
+  const int32_t v = lo >= 0x80000000u ? -(int32_t)(0xFFFFFFFFu - lo) - 1 : (int32_t)lo;
+  return v > 7 ? 7 : (v < -7 ? -7 : (int)v);
 }
 
 #define T_BLOCK 64

@@ -185,7 +185,7 @@ def _extreme_inputs(d, kind):
 
 
 @pytest.mark.parametrize("kind", ["all_min", "all_max", "min_max", "alternating", "zero"])
-@pytest.mark.parametrize("D", [512, 1024])
+@pytest.mark.parametrize("D", [512, 1024, 2048])
 def test_adversarial_extremes(bflib, cuda, oracle, kind, D):
     """Largest |raw J| (|sum| up to 2 * 64 * D) and every G sign: exactness of the tensor path."""
     d = bflib.Dims(128, 2, D, 2, 64)
@@ -292,12 +292,21 @@ def test_resident_weights_and_refresh(bflib, cuda, oracle):
         W.close()
 
 
-def test_full_size_chunk_sampled(bflib, cuda, oracle):
-    """Full single-GPU chunk (t=32768 f=84 d=512 b=96, seed 1): the tensor and
-    SIMT kernels agree on every byte, and two frequencies match the oracle."""
-    d = bflib.Dims(32768, 84, 512, 2, 96)
+def _full_record(golden, shape, seed):
+    g, _ = golden
+    return next(r for r in g["full"] if (r["T"], r["F"], r["D"], r["P"], r["B"], r["seed"]) == (*shape, seed))
+
+
+def test_full_size_chunk_matches_reference(bflib, cuda, golden):
+    """Full single-GPU chunk (t=32768 f=84 d=512 b=96, seed 1): the adler32 of
+    all of J equals the reference cpu.cxx's on the same inputs, and the tensor
+    and SIMT kernels agree on every byte."""
+    shape = (32768, 84, 512, 2, 96)
+    rec = _full_record(golden, shape, 1)
+    d = bflib.Dims(*shape)
     E, A, G = bflib.seeded_host_inputs(d, 1)
     Ed, Ad, Gd = _dev(cuda, E), _dev(cuda, A), _dev(cuda, G)
+    del E
     Jt = cuda.empty(d.jsize, dtype=cuda.uint8, device="cuda")
     Js = cuda.empty(d.jsize, dtype=cuda.uint8, device="cuda")
     bflib.set_kernel("tensor")
@@ -306,17 +315,66 @@ def test_full_size_chunk_sampled(bflib, cuda, oracle):
     bflib.form_beams_ex(d, Js, Ed, Ad, Gd)
     bflib.set_kernel("auto")
     bflib.stream_status()
-    assert bflib.adler32_device(Jt) == bflib.adler32_device(Js)
+    assert bflib.adler32_device(Jt) == rec["adler32"]
     assert cuda.equal(Jt, Js)
-    Jh = Jt.cpu().numpy().reshape(d.nbeams, d.nfrequencies, 2, d.ntimes)
-    E4 = E.reshape(d.ntimes, d.nfrequencies, d.ndishes * 2)
-    for f0 in (0, 83):
-        sub = oracle.Dims(d.ntimes, 1, d.ndishes, 2, d.nbeams)
-        Es = np.ascontiguousarray(E4[:, f0, :]).reshape(-1)
-        As = np.ascontiguousarray(A.reshape(d.nfrequencies, -1)[f0])
-        Gs = np.ascontiguousarray(G.reshape(d.nfrequencies, -1)[f0])
-        Jo = oracle.form_beams(sub, Es, As, Gs).reshape(d.nbeams, 2, d.ntimes)
-        np.testing.assert_array_equal(Jh[:, f0], Jo)
+
+
+def test_wide_array_matches_reference(bflib, cuda, golden):
+    """Wide array (t=16384 f=16 d=1024 b=512, seed 4; six beam passes): adler32
+    of all of J equals the reference cpu.cxx's, on both kernels."""
+    shape = (16384, 16, 1024, 2, 512)
+    rec = _full_record(golden, shape, 4)
+    d = bflib.Dims(*shape)
+    E, A, G = bflib.seeded_host_inputs(d, 4)
+    Ed, Ad, Gd = _dev(cuda, E), _dev(cuda, A), _dev(cuda, G)
+    Jd = cuda.empty(d.jsize, dtype=cuda.uint8, device="cuda")
+    for kernel in ("tensor", "simt"):
+        bflib.set_kernel(kernel)
+        try:
+            bflib.form_beams_ex(d, Jd, Ed, Ad, Gd)
+            bflib.stream_status()
+        finally:
+            bflib.set_kernel("auto")
+        assert bflib.adler32_device(Jd) == rec["adler32"], kernel
+
+
+@pytest.mark.parametrize("name", ["big_gain", "extreme_d2048_all_min", "extreme_d2048_all_max",
+                                  "extreme_d2048_min_max", "extreme_d2048_alternating"])
+def test_edge_case_fixtures(bflib, cuda, golden, name):
+    """The reference's own bytes at the edges of the domain: huge and
+    non-finite gains (int narrowing of cpu.cxx:38 before the clamp) and the
+    deepest dish count of the tensor-core path (d=2048) with extreme inputs
+    (a weight row sum of -2^15, |raw| up to 2 * 64 * d)."""
+    from tests.golden import cases as C
+
+    g, arrays = golden
+    rec = next(r for r in g["cases"] if r["name"] == name)
+    shape, E, A, G = C.make_case(name)
+    d = bflib.Dims(*shape)
+    for kernel in ("tensor", "simt"):
+        J = run_gpu(bflib, cuda, d, E, A, G, kernel)
+        assert bflib.last_kernel() == kernel
+        np.testing.assert_array_equal(J, arrays[rec["array"]], err_msg=kernel)
+
+
+def test_wide_gains_resident_and_plain(bflib, cuda, oracle):
+    """One frequency with huge gains beside ordinary ones: only that
+    frequency takes the narrowing requantisation, in plain launches and with
+    resident weights."""
+    d = bflib.Dims(256, 3, 512, 2, 96)
+    E, A, G = bflib.seeded_host_inputs(d, 44)
+    G = G.copy()
+    G[96:192] = np.float32(3.0e7) * np.linspace(-1, 1, 96, dtype=np.float32)  # frequency 1
+    expect = oracle.form_beams(oracle_dims(oracle, d), E, A, G)
+    np.testing.assert_array_equal(run_gpu(bflib, cuda, d, E, A, G, "tensor"), expect)
+    W = bflib.ResidentWeights(3, 96, 512, A, G)
+    try:
+        Jd = cuda.empty(d.jsize, dtype=cuda.uint8, device="cuda")
+        W.form_beams(Jd, _dev(cuda, E), 256)
+        bflib.stream_status()
+        np.testing.assert_array_equal(Jd.cpu().numpy(), expect)
+    finally:
+        W.close()
 
 
 def test_device_wait_timeout_reports_and_recovers(bflib, cuda, oracle):

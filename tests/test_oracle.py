@@ -100,6 +100,64 @@ def test_seeded_fixtures(oracle, golden):
             np.testing.assert_array_equal(J, arrays[rec["array"]])
 
 
+def test_full_size_fixtures(oracle, golden):
+    """The full single-GPU chunk (t=32768 f=84 d=512 b=96, seed 1) and the
+    wide array (t=16384 f=16 d=1024 b=512, seed 4): the oracle's adler32 over
+    all of J equals the one the reference's own cpu.cxx gave."""
+    g, _ = golden
+    for rec in g["full"]:
+        dims = oracle.Dims(rec["T"], rec["F"], rec["D"], rec["P"], rec["B"])
+        E, A, G = oracle.seeded_inputs(dims, rec["seed"])
+        J = oracle.form_beams(dims, E, A, G)
+        assert oracle.adler32(J) == rec["adler32"], rec
+        del E, J
+
+
+def test_case_fixtures(oracle, golden):
+    """Edge cases (huge and non-finite gains; d=2048 extremes): the oracle
+    gives the reference's own bytes."""
+    from tests.golden import cases as C
+
+    g, arrays = golden
+    assert sorted(r["name"] for r in g["cases"]) == sorted(C.case_names())
+    for rec in g["cases"]:
+        shape, E, A, G = C.make_case(rec["name"])
+        J = oracle.form_beams(oracle.Dims(*shape), E, A, G)
+        np.testing.assert_array_equal(J, arrays[rec["array"]], err_msg=rec["name"])
+
+
+def _narrow_model(g, raw):
+    """int(lrint(g * raw)) clamped to [-7, 7] as the reference's x86-64 build does it."""
+    with np.errstate(invalid="ignore", over="ignore"):
+        x = np.float32(g) * np.float32(raw)
+    if not np.isfinite(x) or abs(float(x)) >= 2.0**63:
+        return 0
+    v = int(np.rint(np.float64(x)))  # a float32 this large is an integer; half-even below
+    v = (v + 2**31) % 2**32 - 2**31
+    return max(-7, min(7, v))
+
+
+def test_requant_narrowing(oracle):
+    """cpu.cxx:38 narrows lrint's long to int before the clamp: products from
+    2^31 up keep their low 32 bits, and NaN / inf / >= 2^63 give 0."""
+    dims = oracle.Dims(16, 1, 64, 2, 16)
+    E, A, _ = oracle.seeded_inputs(dims, 8)
+    G = np.array([2.0**26, -2.0**26, 3.0e7, -5.5e8, 2.0**40 + 2.0**20, 1.0e18, 6.0e18, 1.0e19,
+                  np.inf, -np.inf, np.nan, 2.0**31, 0.75, -1.0e-3, 2.0**-140, 1.0e30], np.float32)
+    J = oracle.form_beams(dims, E, A, G)
+    wrapped = 0
+    for b in range(dims.nbeams):
+        for p in range(2):
+            for t in range(dims.ntimes):
+                re, im = oracle.raw_sum(dims, E, A, b, 0, p, t)
+                want = oracle.encode(_narrow_model(G[b], re), _narrow_model(G[b], im))
+                assert J[(b * 2 + p) * dims.ntimes + t] == want, (b, p, t, G[b], re, im)
+                with np.errstate(invalid="ignore", over="ignore"):
+                    x = float(np.float32(G[b]) * np.float32(re))
+                wrapped += 2.0**31 <= abs(x) < 2.0**63 and _narrow_model(G[b], re) != int(np.sign(x)) * 7
+    assert wrapped > 0  # the narrowing changed some results
+
+
 def test_raw_sum_matches_requant(oracle):
     dims = oracle.Dims(16, 2, 40, 2, 8)
     E, A, G = oracle.seeded_inputs(dims, 4)
