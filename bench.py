@@ -643,6 +643,20 @@ def batched_problems(seed=2, n=128):
     return [(int(t), 1, 512, int(b)) for t, b in zip(ts, bs)]
 
 
+def batched_oracle_check(probs):
+    """Every problem's J (device) against the oracle on the same seeded inputs
+    (seed 2, E stream 2i + 2, A stream 2i + 3); returns how many are equal."""
+    from oracle import oracle as O
+
+    ok = 0
+    for i, (d, _, _, J) in enumerate(probs):
+        od = O.Dims(d.ntimes, d.nfrequencies, d.ndishes, 2, d.nbeams)
+        E = O.fill_random(od.esize, 2, 2 + 2 * i)
+        A = O.fill_random(od.asize, 2, 3 + 2 * i)
+        ok += bool(np.array_equal(J.cpu().numpy(), O.form_beams(od, E, A, O.gains(od))))
+    return ok
+
+
 def run_batched(args):
     """One persistent grouped launch (autotuned, CUDA graph) against the same
     problems launched one by one."""
@@ -678,6 +692,8 @@ def run_batched(args):
     batch.run(stream)
     bf.stream_status(stream)
     assert [bf.adler32_device(J) for _, _, _, J in probs] == ref, "batched launch differs from per-problem launches"
+    oracle_ok = batched_oracle_check(probs)
+    assert oracle_ok == len(probs), f"{len(probs) - oracle_ok} problems differ from the oracle"
 
     def timed(fn):
         for _ in range(max(3, args.warmup)):
@@ -714,7 +730,8 @@ def run_batched(args):
         "speedup_vs_per_problem": round(ms_loop / ms_batch, 3),
         "roofline": roofline_of(bf, stream, total_cmac, alg_bytes, ms_batch, "bf_form_beams_tc (grouped)"),
         "autotune": batch.info(),
-        "parity": "per-problem adler32 of the batched launch equals the per-problem launches",
+        "parity": "every problem's J equals the oracle's (all 128, bytewise) and the per-problem launches' "
+                  "(adler32)",
         "gpu_launches": args.steps,
     }
     print(json.dumps(line), flush=True)
@@ -758,6 +775,16 @@ def served_setup(bf, torch, ncontents):
     for w in per_channel.values():
         w.close()
     torch.cuda.synchronize()
+    # every distinct chunk against the oracle on the host: each landed chunk of
+    # the stream is then checked against a CPU-pinned checksum
+    from oracle import oracle as O
+
+    Ah, Gh = A.cpu().numpy(), G.cpu().numpy()
+    for c, T, Eh, want in contents:
+        od = O.Dims(T, 1, D, 2, B)
+        J = O.form_beams(od, np.ascontiguousarray(Eh), np.ascontiguousarray(Ah[c * B * D:(c + 1) * B * D]),
+                         np.ascontiguousarray(Gh[c * B:(c + 1) * B]))
+        assert O.adler32(J) == want, f"served chunk content (channel {c}, t={T}) differs from the oracle"
     return W, contents
 
 
@@ -927,7 +954,8 @@ def run_served(args):
         "p99_ratio_plain_over_served": round(pl["latency_ms"]["p99"] / sv["latency_ms"]["p99"], 3),
         "saturation_speedup": round(out["served_saturation"]["beam_samples_per_s"]
                                     / out["plain_saturation"]["beam_samples_per_s"], 3),
-        "parity": "every landed chunk's adler32 equals its plain per-chunk launch's",
+        "parity": "every landed chunk's adler32 equals its plain per-chunk launch's, and every distinct chunk's "
+                  "J was checked against the oracle on the host",
         "mismatches": sum(x["mismatches"] for x in (sv, pl, out["served_saturation"], out["plain_saturation"]))
         + sum(x["mismatches"] for x in out.get("load_sweep", [])),
         "clocks": clk,
@@ -964,7 +992,7 @@ def run_wide(args):
     Es = []
     for i in range(NE):
         E = torch.empty(d.esize, dtype=torch.uint8, device="cuda")
-        bf.fill_random_device(E, w["seed"], 2 + i)
+        bf.fill_random_device(E, w["seed"], 0 if i == 0 else 2 + i)  # E 0: the seeded input of the workload
         Es.append(E)
     G = torch.from_numpy(bf.gains(d)).cuda()
     As = []
@@ -982,6 +1010,22 @@ def run_wide(args):
             ref.form_beams(Jt, Es[i], d.ntimes, stream=stream)
             bf.stream_status(stream)
             want[(k, i)] = bf.adler32_device(Jt)
+    # version 0 with E 0 is the seeded workload itself: the reference's cpu.cxx
+    # gave this adler32 (tests/golden/golden.json); one refreshed pair is
+    # checked against the oracle on the host
+    from oracle import oracle as O
+
+    key = tuple(w[k] for k in ("ntimes", "nfrequencies", "ndishes", "npolarizations", "nbeams", "seed"))
+    gpath = os.path.join(ROOT, "tests", "golden", "golden.json")
+    golden = json.load(open(gpath)) if os.path.exists(gpath) else {}
+    ref_rec = next((r for r in golden.get("full", []) if (r["T"], r["F"], r["D"], r["P"], r["B"], r["seed"]) == key),
+                   None)
+    if ref_rec is not None:
+        assert want[(0, 0)] == ref_rec["adler32"], "wide chunk differs from the reference cpu.cxx"
+    od = O.Dims(d.ntimes, d.nfrequencies, d.ndishes, 2, d.nbeams)
+    Jo = O.form_beams(od, Es[1].cpu().numpy(), As[1].cpu().numpy(), G.cpu().numpy())
+    assert O.adler32(Jo) == want[(1, 1)], "refreshed wide chunk differs from the oracle"
+    del Jo
     # kernel alone (version 0 weights), events around each launch
     ref.update(As[0], G, stream=stream)
     for _ in range(3):
@@ -1061,7 +1105,8 @@ def run_wide(args):
                    "latency_ms": {"p50": round(float(np.percentile(lat, 50)) * 1e3, 3),
                                   "p99": round(float(np.percentile(lat, 99)) * 1e3, 3)},
                    "kernel_only_value": d.cmacs / (k_ms * 1e-3)},
-        "parity": "every chunk's adler32 equals a plain launch's with the weights current at its submission",
+        "parity": "every chunk's adler32 equals a plain launch's with the weights current at its submission; "
+                  "(weights 0, E 0) equals the reference cpu.cxx's adler32, (weights 1, E 1) the oracle's",
         "mismatches": int(bad),
         "clocks": clk,
         "gpu_launches": st["batches"],

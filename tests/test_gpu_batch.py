@@ -76,3 +76,28 @@ def test_batch_rejects_mixed_dishes_and_odd_times(bflib, cuda):
     c = _problem(bflib, cuda, 40, 1, 512, 16, 3)
     with pytest.raises(bflib.BeamformError):
         bflib.Batch([(c[2], 40, c[3], c[4])])
+
+
+def test_batched_workload_all_problems(bflib, cuda, oracle):
+    """The batched workload itself (128 problems, f=1 d=512, t log-uniform in
+    [512, 32768], b in {16..128}, seed 2) in one persistent launch: every
+    problem's J equals the oracle's on the same seeded inputs."""
+    import bench
+
+    probs = []
+    for i, (T, F, D, B) in enumerate(bench.batched_problems()):
+        d = bflib.Dims(T, F, D, 2, B)
+        E = cuda.empty(d.esize, dtype=cuda.uint8, device="cuda")
+        A = cuda.empty(d.asize, dtype=cuda.uint8, device="cuda")
+        bflib.fill_random_device(E, 2, 2 + 2 * i)
+        bflib.fill_random_device(A, 2, 3 + 2 * i)
+        W = bflib.ResidentWeights(F, B, D, A, cuda.from_numpy(bflib.gains(d)).cuda())
+        J = cuda.full((d.jsize,), 0x5A, dtype=cuda.uint8, device="cuda")
+        probs.append((d, W, E, J))
+    batch = bflib.Batch([(W, d.ntimes, E, J) for d, W, E, J in probs])
+    batch.run()
+    bflib.stream_status()
+    assert bench.batched_oracle_check(probs) == len(probs)
+    batch.close()
+    for _, W, _, _ in probs:
+        W.close()
