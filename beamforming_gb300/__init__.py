@@ -58,6 +58,7 @@ EXPORTED_SYMBOLS = (
     "bf_batch_create",
     "bf_batch_run",
     "bf_batch_info",
+    "bf_batch_shape",
     "bf_batch_destroy",
     "bf_tensor_peak",
     "bf_form_beams_layout",
@@ -174,6 +175,7 @@ def lib() -> ctypes.CDLL:
         L.bf_batch_create.argtypes = [ctypes.POINTER(vp), ctypes.c_void_p, ctypes.c_int, vp]
         L.bf_batch_run.argtypes = [vp, vp]
         L.bf_batch_info.argtypes = [vp] + [ctypes.POINTER(ctypes.c_int)] * 4 + [ctypes.POINTER(ctypes.c_float)]
+        L.bf_batch_shape.argtypes = [vp] + [ctypes.POINTER(ctypes.c_int)] * 6
         L.bf_batch_destroy.argtypes = [vp]
         L.bf_server_create.argtypes = [ctypes.POINTER(vp), vp, ctypes.POINTER(_ServerConfig)]
         L.bf_server_submit.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int64, u8p, ctypes.c_int, u8p,
@@ -505,9 +507,16 @@ class Batch:
             lib().bf_batch_info(self._h, ctypes.byref(nt), ctypes.byref(order), ctypes.byref(ws), ctypes.byref(raw),
                                 ctypes.byref(ms)),
             "bf_batch_info",
+    "bf_batch_shape",
         )
-        return {"ntiles": nt.value, "order": ("given", "largest_first")[order.value], "wslots": ws.value,
+        info = {"ntiles": nt.value, "order": ("given", "largest_first")[order.value], "wslots": ws.value,
                 "raw_slots": raw.value, "tuned_ms": ms.value}
+        n = ctypes.c_int()
+        arrs = [(ctypes.c_int * 2)() for _ in range(5)]
+        _check(lib().bf_batch_shape(self._h, ctypes.byref(n), *arrs), "bf_batch_shape")
+        names = ("problems", "tiles", "max_nb_pass", "stages", "unpack_groups")
+        info["launches"] = [{k: a[i] for k, a in zip(names, arrs)} for i in range(n.value)]
+        return info
 
     def close(self) -> None:
         if getattr(self, "_h", None):

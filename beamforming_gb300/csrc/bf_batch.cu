@@ -4,25 +4,38 @@
 // frequencies, a number of times, device E and J).  Every problem keeps its own
 // shape -- ntimes and nbeams may all differ; ndishes is shared -- and the
 // tensor-core kernel walks one tile list that spans all of them.  At creation
-// an autotuner times a few schedules (tile order x shared-memory ring plan) on
-// the real buffers and keeps the fastest; the chosen launch is then captured
-// in a CUDA graph, and bf_batch_run() replays it.
+// an autotuner times a few schedules on the real buffers and keeps the
+// fastest: the tile shape (one launch for every problem, or the problems whose
+// beam passes are at most 64 beams wide in a launch of their own, where four
+// or more unpacked stages fit in tensor memory beside narrower accumulators
+// and two unpack groups keep the tensor core fed), the tile order, and the
+// shared-memory ring plan.  The chosen launches are captured in a CUDA graph,
+// and bf_batch_run() replays it.
 #include "bf_internal.h"
 
 #include <algorithm>
 #include <numeric>
 #include <vector>
 
+namespace {
+// One grouped launch of a batch: a range of the device problem table.
+struct BatchLaunch {
+  int first = 0, nprob = 0, ntiles = 0, max_nb_pass = 0, stages = 0, groups = 0;
+};
+}  // namespace
+
 struct bf_batch {
   int device = 0;
   int nprob = 0;
   int ntiles = 0;
-  int max_nb_pass = 0;
   int64_t D = 0;
   int *err = nullptr;
   bf::TcProblem *table = nullptr;  // device copy, launch order
   bf::TcRingPlan plan;
   int order = 0;                   // chosen tile order (0: as given, 1: largest problem first)
+  int split = 0;                   // chosen tile shape (0: one launch, 1: narrow passes apart)
+  int nlaunch = 0;
+  BatchLaunch launches[2];
   float tuned_ms = 0.0f;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -44,19 +57,46 @@ int status_of(cudaError_t e) {
     if (e_ != cudaSuccess) return status_of(e_);   \
   } while (0)
 
-// Problem records in the given order with tile_begin filled in.
-std::vector<TcProblem> ordered(const std::vector<TcProblem> &probs, const std::vector<int> &order, int *ntiles) {
-  std::vector<TcProblem> out;
-  out.reserve(order.size());
-  int64_t begin = 0;
-  for (int i : order) {
-    TcProblem P = probs[i];
-    P.tile_begin = static_cast<int>(begin);
-    begin += tc_problem_tiles(P);
-    out.push_back(P);
+// A schedule: the problem table in launch order (tile_begin counted from the
+// start of each launch) and its launches.
+struct Schedule {
+  std::vector<TcProblem> table;
+  int nlaunch = 0;
+  BatchLaunch launches[2];
+};
+
+// Problems in `order`, split by pass width when `split` (passes wider than
+// kNarrowPass first); empty classes are dropped.
+Schedule schedule_of(const std::vector<TcProblem> &probs, const std::vector<int> &order, bool split) {
+  Schedule sc;
+  for (int cls = 0; cls < (split ? 2 : 1); ++cls) {
+    BatchLaunch L;
+    L.first = static_cast<int>(sc.table.size());
+    int64_t begin = 0;
+    for (int i : order) {
+      const bool narrow = probs[i].nb_pass <= kNarrowPass;
+      if (split && narrow != (cls == 1)) continue;
+      TcProblem P = probs[i];
+      P.tile_begin = static_cast<int>(begin);
+      begin += tc_problem_tiles(P);
+      L.max_nb_pass = std::max(L.max_nb_pass, P.nb_pass);
+      sc.table.push_back(P);
+    }
+    L.nprob = static_cast<int>(sc.table.size()) - L.first;
+    L.ntiles = static_cast<int>(begin);
+    if (L.nprob > 0) sc.launches[sc.nlaunch++] = L;
   }
-  *ntiles = static_cast<int>(begin);
-  return out;
+  return sc;
+}
+
+cudaError_t launch_schedule(const bf_batch *b, const BatchLaunch *ls, int n, const TcRingPlan &plan,
+                            cudaStream_t s) {
+  for (int i = 0; i < n; ++i) {
+    const cudaError_t e =
+        launch_tc_grouped(b->table + ls[i].first, ls[i].nprob, ls[i].ntiles, b->D, ls[i].max_nb_pass, plan, b->err, s);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 }  // namespace
@@ -68,7 +108,7 @@ int bf_batch_create(bf_batch **out, const bf_problem *problems, int nproblems, b
   *out = nullptr;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   int64_t D = -1;
-  int max_nb = 0;
+  int max_nb = 0, min_nb = 1 << 30;
   std::vector<TcProblem> probs(static_cast<size_t>(nproblems));
   for (int i = 0; i < nproblems; ++i) {
     const bf_problem &q = problems[i];
@@ -80,6 +120,7 @@ int bf_batch_create(bf_batch **out, const bf_problem *problems, int nproblems, b
     if ((reinterpret_cast<uintptr_t>(q.E) | reinterpret_cast<uintptr_t>(q.J)) & 15u) return BF_ERR_UNSUPPORTED;
     BF_TRY(tc_make_problem(probs[i], w, q.ntimes, q.J, q.E, 0));
     max_nb = std::max(max_nb, w.nb_pass);
+    min_nb = std::min(min_nb, w.nb_pass);
   }
   int *err = nullptr;
   int st = device_error_word(&err);
@@ -88,7 +129,6 @@ int bf_batch_create(bf_batch **out, const bf_problem *problems, int nproblems, b
   bf_batch *b = new bf_batch();
   cudaGetDevice(&b->device);
   b->nprob = nproblems;
-  b->max_nb_pass = max_nb;
   b->D = D;
   b->err = err;
   if (cudaMalloc(&b->table, sizeof(TcProblem) * nproblems) != cudaSuccess) {
@@ -96,8 +136,9 @@ int bf_batch_create(bf_batch **out, const bf_problem *problems, int nproblems, b
     return BF_ERR_OUT_OF_MEMORY;
   }
 
-  // Autotune: tile order x ring plan, each timed on the real buffers (every
-  // candidate writes the same J, so the outputs are valid afterwards).
+  // Autotune: tile shape x tile order x ring plan, each timed on the real
+  // buffers (every candidate writes the same J, so the outputs are valid
+  // afterwards).  Splitting only applies when both pass classes are present.
   std::vector<int> given(static_cast<size_t>(nproblems));
   std::iota(given.begin(), given.end(), 0);
   std::vector<int> largest = given;
@@ -105,6 +146,7 @@ int bf_batch_create(bf_batch **out, const bf_problem *problems, int nproblems, b
     return tc_problem_tiles(probs[x]) > tc_problem_tiles(probs[y]);
   });
   const std::vector<int> *orders[2] = {&given, &largest};
+  const int nsplit = (min_nb <= kNarrowPass && max_nb > kNarrowPass) ? 2 : 1;
   TcRingPlan plans[3];
   plans[1].wslots = 4;
   plans[1].raw = 8;
@@ -115,51 +157,59 @@ int bf_batch_create(bf_batch **out, const bf_problem *problems, int nproblems, b
   cudaEventCreate(&e1);
   float best = -1.0f;
   st = BF_OK;
-  for (int o = 0; o < 2 && st == BF_OK; ++o) {
-    int ntiles = 0;
-    const std::vector<TcProblem> table = ordered(probs, *orders[o], &ntiles);
-    cudaError_t e = cudaMemcpyAsync(b->table, table.data(), sizeof(TcProblem) * table.size(),
-                                    cudaMemcpyHostToDevice, s);
-    for (int pl = 0; pl < 3 && e == cudaSuccess; ++pl) {
-      e = launch_tc_grouped(b->table, nproblems, ntiles, D, max_nb, plans[pl], err, s);  // warm-up
-      if (e != cudaSuccess) break;
-      cudaEventRecord(e0, s);
-      for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep)
-        e = launch_tc_grouped(b->table, nproblems, ntiles, D, max_nb, plans[pl], err, s);
-      cudaEventRecord(e1, s);
-      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-      float ms = 0.0f;
-      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
-      if (e == cudaSuccess && (best < 0.0f || ms < best)) {
-        best = ms;
-        b->order = o;
-        b->plan = plans[pl];
-        b->ntiles = ntiles;
+  for (int sp = 0; sp < nsplit && st == BF_OK; ++sp) {
+    for (int o = 0; o < 2 && st == BF_OK; ++o) {
+      const Schedule sc = schedule_of(probs, *orders[o], sp == 1);
+      cudaError_t e = cudaMemcpyAsync(b->table, sc.table.data(), sizeof(TcProblem) * sc.table.size(),
+                                      cudaMemcpyHostToDevice, s);
+      for (int pl = 0; pl < 3 && e == cudaSuccess; ++pl) {
+        e = launch_schedule(b, sc.launches, sc.nlaunch, plans[pl], s);  // warm-up
+        if (e != cudaSuccess) break;
+        cudaEventRecord(e0, s);
+        for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) e = launch_schedule(b, sc.launches, sc.nlaunch, plans[pl], s);
+        cudaEventRecord(e1, s);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e == cudaSuccess && (best < 0.0f || ms < best)) {
+          best = ms;
+          b->split = sp;
+          b->order = o;
+          b->plan = plans[pl];
+        }
       }
+      if (e != cudaSuccess) st = status_of(e);
     }
-    if (e != cudaSuccess) st = status_of(e);
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (st == BF_OK) {
-    int ntiles = 0;
-    const std::vector<TcProblem> table = ordered(probs, *orders[b->order], &ntiles);
+    const Schedule sc = schedule_of(probs, *orders[b->order], b->split == 1);
     b->tuned_ms = best / 3.0f;
-    cudaError_t e = cudaMemcpyAsync(b->table, table.data(), sizeof(TcProblem) * table.size(),
+    b->nlaunch = sc.nlaunch;
+    b->ntiles = 0;
+    for (int i = 0; i < sc.nlaunch; ++i) {
+      b->launches[i] = sc.launches[i];
+      b->ntiles += sc.launches[i].ntiles;
+      if (tc_launch_shape(D, b->launches[i].max_nb_pass, b->plan, &b->launches[i].stages, &b->launches[i].groups) !=
+          cudaSuccess)
+        st = BF_ERR_UNSUPPORTED;
+    }
+    cudaError_t e = cudaMemcpyAsync(b->table, sc.table.data(), sizeof(TcProblem) * sc.table.size(),
                                     cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    // capture the chosen launch in a graph
+    // capture the chosen launches in a graph
     cudaStream_t cap = nullptr;
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-      const cudaError_t le = launch_tc_grouped(b->table, nproblems, ntiles, D, max_nb, b->plan, err, cap);
+      const cudaError_t le = launch_schedule(b, b->launches, b->nlaunch, b->plan, cap);
       e = cudaStreamEndCapture(cap, &b->graph);
       if (le != cudaSuccess) e = le;
     }
     if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
     if (cap) cudaStreamDestroy(cap);
-    if (e != cudaSuccess) st = status_of(e);
+    if (e != cudaSuccess && st == BF_OK) st = status_of(e);
   }
   if (st != BF_OK) {
     bf_batch_destroy(b);
@@ -181,6 +231,21 @@ int bf_batch_info(const bf_batch *b, int *ntiles, int *order, int *wslots, int *
   if (wslots) *wslots = b->plan.wslots;
   if (raw) *raw = b->plan.raw;
   if (tuned_ms) *tuned_ms = b->tuned_ms;
+  return BF_OK;
+}
+
+int bf_batch_shape(const bf_batch *b, int *nlaunches, int *nproblems, int *ntiles, int *max_nb_pass, int *stages,
+                   int *unpack_groups) {
+  if (!b || !nlaunches) return BF_ERR_INVALID_ARGUMENT;
+  *nlaunches = b->nlaunch;
+  for (int i = 0; i < b->nlaunch; ++i) {
+    const BatchLaunch &L = b->launches[i];
+    if (nproblems) nproblems[i] = L.nprob;
+    if (ntiles) ntiles[i] = L.ntiles;
+    if (max_nb_pass) max_nb_pass[i] = L.max_nb_pass;
+    if (stages) stages[i] = L.stages;
+    if (unpack_groups) unpack_groups[i] = L.groups;
+  }
   return BF_OK;
 }
 

@@ -168,6 +168,13 @@ int tc_stages_per_tile(int64_t D);
 cudaError_t launch_tc_grouped(const TcProblem *table, int nprob, int ntiles, int64_t D, int max_nb_pass,
                               const TcRingPlan &plan, int *err, cudaStream_t s);
 
+// TMEM stages and unpack groups a grouped launch with these sizes would use.
+cudaError_t tc_launch_shape(int64_t D, int max_nb_pass, const TcRingPlan &plan, int *stages, int *groups);
+
+// Beam passes of at most this many beams leave room for four or more unpacked
+// stages in TMEM, and so for two unpack groups.
+constexpr int kNarrowPass = 64;
+
 // Failure-path test hook: nonzero makes the producer of later tensor-core
 // launches issue nothing, so the kernel's bounded waits expire.
 void tc_set_test_stall(int on);

@@ -40,6 +40,12 @@
 //                de-interleaved E4M3 operand rows written straight into tensor
 //                memory (tcgen05.st); no shared-memory operand
 //
+// Launches with four or more unpacked stages in TMEM (beam passes of at most
+// 64 beams) run two unpack groups, which take the stages in turn, and one more
+// warp, the W forwarder: it arrives on a stage's a_full once that stage's W slot
+// has landed, so the unpack warps carry no W hand-over, and the W producer
+// reuses a slot as soon as the tensor core has finished the stage that used it.
+//
 // GEMM row r of a tile (TMEM lane r) is (t, p) = (r / 2, r % 2) for the 64 times
 // of the tile.  TMEM columns: accumulators at [0, N) and [256, 256 + N), unpacked
 // E stages (64 columns = 256 K bytes each) in the remaining columns.
@@ -61,17 +67,19 @@ namespace {
 // fours covering the four lane quarters.  Twelve epilogue warps suit short K
 // (ndishes <= 512: the epilogue paces the tiles), eight suit long K (the
 // unpack does, and more epilogue warps take its issue slots).
-template <int kEpiWarps_>
+template <int kEpiWarps_, int kUnpackGroups_>
 struct Roles {
   static constexpr int kEpiWarps = kEpiWarps_;
-  static constexpr int kUnpackGroups = 1;
+  static constexpr int kUnpackGroups = kUnpackGroups_;
+  static constexpr bool kForwarder = kUnpackGroups > 1;  // W-landed forwarder warp
   static constexpr int kEpiThreads = 32 * kEpiWarps;
   static constexpr int kEpiParts = kEpiWarps / 4;  // column parts: each read by four warps (one per lane quarter)
   static constexpr int kEProdWarp = kEpiWarps;
   static constexpr int kMmaWarp = kEpiWarps + 1;
   static constexpr int kWProdWarp = kEpiWarps + 2;
   static constexpr int kUnpackWarp0 = kEpiWarps + 3;
-  static constexpr int kThreads = 32 * (kUnpackWarp0 + 4 * kUnpackGroups);
+  static constexpr int kFwdWarp = kUnpackWarp0 + 4 * kUnpackGroups;
+  static constexpr int kThreads = 32 * (kFwdWarp + (kForwarder ? 1 : 0));
 };
 constexpr int kTT = 64;                 // times per tile
 constexpr int kBM = 128;                // GEMM rows per tile
@@ -111,6 +119,7 @@ struct TcParams {
   int wslots;               // W slots in smem
   int raw;                  // raw E slots in smem
   int test_stall;           // nonzero: the producers issue nothing (failure-path test)
+  int groups;               // unpack groups (2: with the W forwarder; needs stages >= 4)
   int *err;
 };
 
@@ -263,9 +272,10 @@ __device__ __forceinline__ uint32_t sw128_offset(uint32_t r, uint32_t j) {
   return (r >> 3) * 1024u + (r & 7u) * 128u + ((j ^ (r & 7u)) << 4);
 }
 
-template <bool kGrouped, bool kJ2, int kEpiW, bool kAdler>
-__global__ void __launch_bounds__(Roles<kEpiW>::kThreads, 1) bf_form_beams_tc(const __grid_constant__ TcParams p) {
-  using RL = Roles<kEpiW>;
+template <bool kGrouped, bool kJ2, int kEpiW, bool kAdler, int kGroups>
+__global__ void __launch_bounds__(Roles<kEpiW, kGroups>::kThreads, 1)
+    bf_form_beams_tc(const __grid_constant__ TcParams p) {
+  using RL = Roles<kEpiW, kGroups>;
   constexpr int kEpiThreads = RL::kEpiThreads, kEpiParts = RL::kEpiParts, kEProdWarp = RL::kEProdWarp;
   constexpr int kMmaWarp = RL::kMmaWarp, kWProdWarp = RL::kWProdWarp, kUnpackWarp0 = RL::kUnpackWarp0;
   constexpr int kUnpackGroups = RL::kUnpackGroups;
@@ -305,7 +315,7 @@ __global__ void __launch_bounds__(Roles<kEpiW>::kThreads, 1) bf_form_beams_tc(co
       mbar_init(w_empty(s), 1);
     }
     for (int s = 0; s < S; ++s) {
-      mbar_init(a_full(s), 128);
+      mbar_init(a_full(s), 128 + (RL::kForwarder ? 1 : 0));  // one unpack group (+ the W forwarder)
       mbar_init(empty(s), 1);
     }
     for (int i = 0; i < 2; ++i) {
@@ -416,7 +426,19 @@ __global__ void __launch_bounds__(Roles<kEpiW>::kThreads, 1) bf_form_beams_tc(co
         }
         for (int ks = 0; ks < p.nk; ++ks, ++it, wr.advance()) {
           const int s = static_cast<int>(wr.idx);
-          if (!mbar_wait(w_empty(s), wr.phase ^ 1u, err, kDevTimeoutEmpty)) {
+          if constexpr (RL::kForwarder) {
+            // the slot held sequence it - SW: free once the tensor core finished
+            // that stage (its commit on empty).  SW <= 2 S, so that barrier cannot
+            // have moved two phases past the one waited for.
+            if (it >= static_cast<uint32_t>(SW)) {
+              const uint32_t j = it - static_cast<uint32_t>(SW);
+              if (!mbar_wait(empty(static_cast<int>(j % static_cast<uint32_t>(S))), (j / static_cast<uint32_t>(S)) & 1u,
+                             err, kDevTimeoutEmpty)) {
+                ok = false;
+                break;
+              }
+            }
+          } else if (!mbar_wait(w_empty(s), wr.phase ^ 1u, err, kDevTimeoutEmpty)) {
             ok = false;
             break;
           }
@@ -476,6 +498,21 @@ __global__ void __launch_bounds__(Roles<kEpiW>::kThreads, 1) bf_form_beams_tc(co
         }
         if (!ok) break;
         mma_commit(accfull(ab));
+      }
+    }
+  } else if (RL::kForwarder && warp == RL::kFwdWarp) {
+    // ------------------------------------------------------------ W forwarder
+    // Sequence it's a_full gets one arrival from here once its W slot has
+    // landed, after the previous use of that a_full slot (it - S) completed.
+    if (lane == 0 && !p.test_stall) {
+      const uint32_t total = TileRange::of<kGrouped>(p).count() * static_cast<uint32_t>(p.nk);
+      const uint32_t uS = static_cast<uint32_t>(S), uSW = static_cast<uint32_t>(SW);
+      for (uint32_t it = 0; it < total; ++it) {
+        if (!mbar_wait(w_full(static_cast<int>(it % uSW)), (it / uSW) & 1u, err, kDevTimeoutFull)) break;
+        if (it >= uS &&
+            !mbar_wait(a_full(static_cast<int>((it - uS) % uS)), ((it - uS) / uS) & 1u, err, kDevTimeoutUnpacked))
+          break;
+        mbar_arrive(a_full(static_cast<int>(it % uS)));
       }
     }
   } else if (warp >= kUnpackWarp0) {
@@ -550,8 +587,10 @@ __global__ void __launch_bounds__(Roles<kEpiW>::kThreads, 1) bf_form_beams_tc(co
         // the stores first: the W-slot hand-over runs while they drain
 #pragma unroll
         for (int h = 0; h < kSub; ++h) tmem_st_32x32b_x32(col + 32 * h, out[h]);
-        if (it >= static_cast<uint32_t>(S) && wlead) mbar_arrive(w_empty(relslot));  // sequence it - S is done
-        if (wlead && !mbar_wait(w_full(static_cast<int>(wr.idx)), wr.phase, err, kDevTimeoutFull)) ok = false;
+        if constexpr (!RL::kForwarder) {
+          if (it >= static_cast<uint32_t>(S) && wlead) mbar_arrive(w_empty(relslot));  // sequence it - S is done
+          if (wlead && !mbar_wait(w_full(static_cast<int>(wr.idx)), wr.phase, err, kDevTimeoutFull)) ok = false;
+        }
         tmem_st_wait();
         if (!__all_sync(0xffffffffu, ok)) break;
         tc_fence_before();
@@ -963,45 +1002,59 @@ static cudaError_t plan_launch(TcParams &p, int max_nb_pass, const TcRingPlan &p
   while (raw < kMaxRaw && smem_plan(stages, wslots, raw + 1, max_nb_pass).total + 1024 <= kSmemLimit && want_r <= 0)
     ++raw;
   while (raw > 2 && smem_plan(stages, wslots, raw, max_nb_pass).total + 1024 > kSmemLimit) --raw;
-  // the unpack hands W slots back S stages late: at least S slots keep it moving
-  const int st = std::min(stages, wslots);
+  // Four or more unpacked stages: two unpack groups and the W forwarder, whose
+  // W slots are reused straight after the tensor core's release (this needs
+  // SW <= 2 S, true for every plan here).  Otherwise one group, which hands W
+  // slots back S stages late, so at least S slots keep it moving.
+  const int groups = stages >= 4 ? 2 : 1;
+  const int st = groups == 2 ? stages : std::min(stages, wslots);
+  if (groups == 2 && wslots > 2 * st) return cudaErrorInvalidValue;
   p.max_nb_pass = max_nb_pass;
   p.stages = st;
   p.wslots = wslots;
   p.raw = raw;
+  p.groups = groups;
   p.test_stall = g_test_stall;
   *smem_bytes = smem_plan(st, wslots, raw, max_nb_pass).total + 1024;
   return *smem_bytes > kSmemLimit ? cudaErrorInvalidValue : cudaSuccess;
 }
 
-template <bool kGrouped, bool kJ2, int kEpiW, bool kAdler>
+template <bool kGrouped, bool kJ2, int kEpiW, bool kAdler, int kGroups>
 static cudaError_t launch_inst(const TcParams &p, int smem_bytes, cudaStream_t s) {
   static std::atomic<bool> attr_set{false};
   if (!attr_set.load()) {
-    const cudaError_t e = cudaFuncSetAttribute(bf_form_beams_tc<kGrouped, kJ2, kEpiW, kAdler>,
+    const cudaError_t e = cudaFuncSetAttribute(bf_form_beams_tc<kGrouped, kJ2, kEpiW, kAdler, kGroups>,
                                                cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
     if (e != cudaSuccess) return e;
     attr_set.store(true);
   }
   const int grid = std::min(p.ntiles, num_sms());
   if (grid <= 0) return cudaSuccess;
-  bf_form_beams_tc<kGrouped, kJ2, kEpiW, kAdler><<<grid, Roles<kEpiW>::kThreads, smem_bytes, s>>>(p);
+  bf_form_beams_tc<kGrouped, kJ2, kEpiW, kAdler, kGroups><<<grid, Roles<kEpiW, kGroups>::kThreads, smem_bytes, s>>>(p);
   return cudaGetLastError();
+}
+
+// Warp layout of a launch: two unpack groups (with the forwarder) beside eight
+// epilogue warps; one group beside twelve epilogue warps up to 4 K stages per
+// tile (the epilogue paces short tiles) or eight for deeper tiles.
+template <bool kGrouped, bool kJ2, bool kAdler>
+static cudaError_t launch_layout(const TcParams &p, int smem_bytes, cudaStream_t s) {
+  if (p.groups == 2) return launch_inst<kGrouped, kJ2, 8, kAdler, 2>(p, smem_bytes, s);
+  return p.nk <= 4 ? launch_inst<kGrouped, kJ2, 12, kAdler, 1>(p, smem_bytes, s)
+                   : launch_inst<kGrouped, kJ2, 8, kAdler, 1>(p, smem_bytes, s);
 }
 
 template <bool kJ2, bool kAdler>
 static cudaError_t launch_plain(const TcParams &p, int smem_bytes, cudaStream_t s) {
-  return p.nk <= 4 ? launch_inst<false, kJ2, 12, kAdler>(p, smem_bytes, s)
-                   : launch_inst<false, kJ2, 8, kAdler>(p, smem_bytes, s);
+  return launch_layout<false, kJ2, kAdler>(p, smem_bytes, s);
 }
 
 // Instantiation for a launch: J2 output and the fused adler32 only in plain
-// launches; the epilogue width by the K stages per tile (12 warps up to 4).
+// launches.
 template <bool kGrouped>
 static cudaError_t launch_kernel(const TcParams &p, int smem_bytes, cudaStream_t s) {
   if constexpr (kGrouped) {
-    return p.nk <= 4 ? launch_inst<true, false, 12, false>(p, smem_bytes, s)
-                     : launch_inst<true, false, 8, false>(p, smem_bytes, s);
+    return launch_layout<true, false, false>(p, smem_bytes, s);
   } else {
     const bool j2 = p.one.jlayout == kJ2, adler = p.one.adler != nullptr;
     if (j2) return adler ? launch_plain<true, true>(p, smem_bytes, s) : launch_plain<true, false>(p, smem_bytes, s);
@@ -1017,6 +1070,17 @@ cudaError_t tc_make_problem(TcProblem &P, const TcWeights &w, int64_t T, uint8_t
 int64_t tc_problem_tiles(const TcProblem &P) { return static_cast<int64_t>(P.ntt) * P.F * P.npass; }
 
 int tc_stages_per_tile(int64_t D) { return static_cast<int>((D + kStageK / 2 - 1) / (kStageK / 2)); }
+
+cudaError_t tc_launch_shape(int64_t D, int max_nb_pass, const TcRingPlan &plan, int *stages, int *groups) {
+  TcParams p{};
+  p.nk = tc_stages_per_tile(D);
+  int smem_bytes = 0;
+  const cudaError_t e = plan_launch(p, max_nb_pass, plan, &smem_bytes);
+  if (e != cudaSuccess) return e;
+  *stages = p.stages;
+  *groups = p.groups;
+  return cudaSuccess;
+}
 
 cudaError_t launch_tc_grouped(const TcProblem *table, int nprob, int ntiles, int64_t D, int max_nb_pass,
                               const TcRingPlan &plan, int *err, cudaStream_t s) {

@@ -7,16 +7,16 @@
  *                             clamp(int(lrint(G[f][b] * float(im))), -7, 7))
  *   re + i*im    = sum_d A[f][b][d] * E[t][f][d][p]        (exact integers)
  *
+ * over 4-bit complex data stored as ucomplex4 bytes (real part in the high
+ * nibble, imaginary part in the low nibble, each stored as value + 8).  The
+ * result is bit-identical to the reference CPU implementation
+ * (eschnett/beamforming cpu.cxx:15-46).
+ *
  * As in cpu.cxx:38, lrint's 64-bit result is narrowed to int before the
  * clamp: a product with 2^31 <= |G * raw| < 2^63 keeps its low 32 bits (so it
  * clamps to 0, +7 or -7 by those bits), and a NaN, infinite or |G * raw| >= 2^63
  * product gives 0 (what the reference's x86-64 build returns).  Any float G is
  * accepted.
- *
- * over 4-bit complex data stored as ucomplex4 bytes (real part in the high
- * nibble, imaginary part in the low nibble, each stored as value + 8).  The
- * result is bit-identical to the reference CPU implementation
- * (eschnett/beamforming cpu.cxx:15-46).
  *
  * Array layouts (all byte arrays, C order) follow the reference accessors:
  *   E[t][f][d][p]   Elinear   arraysizes.hxx:80
@@ -162,8 +162,12 @@ typedef struct bf_problem {
 } bf_problem;
 
 /* Builds a batch: times a few launch schedules on the given buffers (tile
- * order x shared-memory ring plan), keeps the fastest and captures it in a
- * CUDA graph.  The buffers must stay allocated while the batch exists; their
+ * shape x tile order x shared-memory ring plan), keeps the fastest and
+ * captures it in a CUDA graph.  The tile shape is either one persistent
+ * launch over every problem, or -- when the batch mixes beam passes wider and
+ * narrower than 64 beams -- the narrow ones in a launch of their own, whose
+ * smaller accumulators leave tensor memory for four or more unpacked stages
+ * and two unpack warp groups.  The buffers must stay allocated while the batch exists; their
  * contents may change between runs.  Each problem needs the tensor-core shape
  * rules (ntimes % 16 == 0, ndishes % 8 == 0, ndishes <= 2048, 16-byte aligned E and J). */
 BF_API int bf_batch_create(bf_batch **out, const bf_problem *problems, int nproblems, bf_stream_t stream);
@@ -174,6 +178,13 @@ BF_API int bf_batch_run(bf_batch *batch, bf_stream_t stream);
 /* The schedule the autotuner chose: tiles, tile order (0 as given, 1 largest
  * problem first), ring plan (0 = default) and the tuned time of one run. */
 BF_API int bf_batch_info(const bf_batch *batch, int *ntiles, int *order, int *wslots, int *raw, float *tuned_ms);
+
+/* The tile shape the autotuner chose: the number of launches (1 or 2) and,
+ * per launch (arrays of at least 2 entries, any of them may be NULL), its
+ * problems, tiles, widest beam pass, unpacked stages in tensor memory and
+ * unpack warp groups.  No counterpart in the reference. */
+BF_API int bf_batch_shape(const bf_batch *batch, int *nlaunches, int *nproblems, int *ntiles, int *max_nb_pass,
+                          int *stages, int *unpack_groups);
 
 BF_API int bf_batch_destroy(bf_batch *batch);
 

@@ -67,6 +67,22 @@ def test_batch_replay_sees_new_inputs(bflib, cuda, oracle):
     batch.close()
 
 
+def test_batch_narrow_passes_two_groups(bflib, cuda, oracle):
+    """Only passes of at most 64 beams (b = 16, 40, 64, and 128 as two passes of
+    64): one grouped launch with four or more unpacked stages and two unpack
+    groups; every problem equals the oracle."""
+    shapes = [(512, 1, 512, 16), (208, 2, 512, 40), (1024, 1, 512, 64), (256, 2, 512, 128), (64, 1, 512, 8)]
+    probs = [_problem(bflib, cuda, T, F, D, B, 300 + i) for i, (T, F, D, B) in enumerate(shapes)]
+    batch = bflib.Batch([(W, d.ntimes, Ed, Jd) for d, _, W, Ed, Jd in probs])
+    (L,) = batch.info()["launches"]
+    assert L["stages"] >= 4 and L["unpack_groups"] == 2 and L["max_nb_pass"] == 64
+    batch.run()
+    bflib.stream_status()
+    for d, (E, A, G), W, Ed, Jd in probs:
+        np.testing.assert_array_equal(Jd.cpu().numpy(), _oracle(oracle, d, E, A, G), err_msg=str(d))
+    batch.close()
+
+
 def test_batch_rejects_mixed_dishes_and_odd_times(bflib, cuda):
     a = _problem(bflib, cuda, 64, 1, 512, 16, 1)
     b = _problem(bflib, cuda, 64, 1, 256, 16, 2)
@@ -95,6 +111,13 @@ def test_batched_workload_all_problems(bflib, cuda, oracle):
         J = cuda.full((d.jsize,), 0x5A, dtype=cuda.uint8, device="cuda")
         probs.append((d, W, E, J))
     batch = bflib.Batch([(W, d.ntimes, E, J) for d, W, E, J in probs])
+    info = batch.info()
+    launches = info["launches"]
+    assert 1 <= len(launches) <= 2 and sum(L["problems"] for L in launches) == len(probs)
+    assert sum(L["tiles"] for L in launches) == info["ntiles"]
+    for L in launches:  # four or more unpacked stages run two unpack groups
+        assert L["unpack_groups"] == (2 if L["stages"] >= 4 else 1)
+        assert (L["stages"] >= 4) == (L["max_nb_pass"] <= 64)
     batch.run()
     bflib.stream_status()
     assert bench.batched_oracle_check(probs) == len(probs)

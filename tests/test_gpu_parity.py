@@ -377,10 +377,12 @@ def test_wide_gains_resident_and_plain(bflib, cuda, oracle):
         W.close()
 
 
-def test_device_wait_timeout_reports_and_recovers(bflib, cuda, oracle):
+@pytest.mark.parametrize("B", [96, 32])
+def test_device_wait_timeout_reports_and_recovers(bflib, cuda, oracle, B):
     """A launch whose copies are never issued: its bounded waits expire, the
-    call reports ERR_DEVICE_TIMEOUT, and the next launch is correct."""
-    d = bflib.Dims(128, 2, 512, 2, 96)
+    call reports ERR_DEVICE_TIMEOUT, and the next launch is correct (b=96: one
+    unpack group; b=32: two groups and the W forwarder)."""
+    d = bflib.Dims(128, 2, 512, 2, B)
     E, A, G = bflib.seeded_host_inputs(d, 9)
     bflib.set_test_stall(True)
     try:
