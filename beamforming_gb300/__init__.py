@@ -507,7 +507,6 @@ class Batch:
             lib().bf_batch_info(self._h, ctypes.byref(nt), ctypes.byref(order), ctypes.byref(ws), ctypes.byref(raw),
                                 ctypes.byref(ms)),
             "bf_batch_info",
-    "bf_batch_shape",
         )
         info = {"ntiles": nt.value, "order": ("given", "largest_first")[order.value], "wslots": ws.value,
                 "raw_slots": raw.value, "tuned_ms": ms.value}
