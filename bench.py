@@ -66,6 +66,8 @@ def parse_args():
     ap.add_argument("--rounds", type=int, default=6, help="wide: rounds (J checked between rounds)")
     ap.add_argument("--rate", type=float, default=None, help="served: arrival rate (chunks/s)")
     ap.add_argument("--duration", type=float, default=None, help="served: stream length (s)")
+    ap.add_argument("--repeats", type=int, default=1, help="served: repeats of the stream and saturation runs, "
+                    "served and plain interleaved")
     ap.add_argument("--contents", type=int, default=128, help="served: distinct chunks the stream draws from")
     ap.add_argument("--slots", type=int, default=512, help="served: pinned J slots in the ring")
     ap.add_argument("--check-threads", type=int, default=6, help="served: threads checking landed chunks")
@@ -887,6 +889,20 @@ def serve_stream(bf, torch, W, contents, arrivals, picks, cfg, nslots, check_thr
     }
 
 
+def repeat_spread(reps):
+    """Per loop, every repeat's p50 / p99 / p99.9 latency (ms) and beam
+    samples/s, with their min / median / max."""
+    out = {}
+    for name, runs in reps.items():
+        d = {"beam_samples_per_s": [r["beam_samples_per_s"] for r in runs]}
+        if "latency_ms" in runs[0]:
+            for q in ("p50", "p99", "p99.9"):
+                d[q] = [r["latency_ms"][q] for r in runs]
+        out[name] = {k: {"runs": v, "min": min(v), "median": statistics.median(v), "max": max(v)}
+                     for k, v in d.items()}
+    return out
+
+
 def run_served(args):
     """The served stream against the plain per-chunk loop (the same server
     thread with one chunk per launch and one launch in flight), at the
@@ -910,15 +926,21 @@ def run_served(args):
     served_cfg = {"max_batch": args.max_batch, "max_inflight": args.max_inflight, "spin_wait": not args.no_spin}
     plain_cfg = {"max_batch": 1, "max_inflight": 1, "spin_wait": not args.no_spin}
     out = {}
+    reps = {k: [] for k in ("served", "plain", "served_saturation", "plain_saturation")}
     clocks = ClockSampler(gpu_uuid(torch, 0))
     clocks.start()
     for name, cfg in (("served", served_cfg), ("plain", plain_cfg)):
         serve_stream(bf, torch, W, contents, np.zeros(min(200, n)), picks[:200], cfg, args.slots,
                      args.check_threads)  # warm-up
-        out[name] = serve_stream(bf, torch, W, contents, arrivals, picks, cfg, args.slots, args.check_threads)
-        out[name + "_saturation"] = serve_stream(bf, torch, W, contents, np.zeros(nsat), sat_picks, cfg, nsat,
-                                                 args.check_threads)
-        del out[name + "_saturation"]["submit_lateness_ms"]  # every chunk is due at once
+    for rep in range(max(1, args.repeats)):  # the two loops interleaved, the same arrivals every time
+        for name, cfg in (("served", served_cfg), ("plain", plain_cfg)):
+            reps[name].append(serve_stream(bf, torch, W, contents, arrivals, picks, cfg, args.slots,
+                                           args.check_threads))
+            r = serve_stream(bf, torch, W, contents, np.zeros(nsat), sat_picks, cfg, nsat, args.check_threads)
+            del r["submit_lateness_ms"]  # every chunk is due at once
+            reps[name + "_saturation"].append(r)
+    for k, v in reps.items():
+        out[k] = v[0]
     for rate_x in args.extra_rates:
         nx = int(round(rate_x * args.extra_duration))
         arr_x = np.cumsum(rng.exponential(1.0 / rate_x, nx))
@@ -954,10 +976,13 @@ def run_served(args):
         "p99_ratio_plain_over_served": round(pl["latency_ms"]["p99"] / sv["latency_ms"]["p99"], 3),
         "saturation_speedup": round(out["served_saturation"]["beam_samples_per_s"]
                                     / out["plain_saturation"]["beam_samples_per_s"], 3),
+        "repeats": repeat_spread(reps),
         "parity": "every landed chunk's adler32 equals its plain per-chunk launch's, and every distinct chunk's "
                   "J was checked against the oracle on the host",
-        "mismatches": sum(x["mismatches"] for x in (sv, pl, out["served_saturation"], out["plain_saturation"]))
+        "mismatches": sum(x["mismatches"] for v in reps.values() for x in v)
         + sum(x["mismatches"] for x in out.get("load_sweep", [])),
+        "chunks_checked": sum(x["chunks"] for v in reps.values() for x in v)
+        + sum(x["chunks"] for x in out.get("load_sweep", [])),
         "clocks": clk,
         "gpu_launches": sv["server"]["batches"],
     }
