@@ -66,6 +66,8 @@ def parse_args():
     ap.add_argument("--rounds", type=int, default=6, help="wide: rounds (J checked between rounds)")
     ap.add_argument("--rate", type=float, default=None, help="served: arrival rate (chunks/s)")
     ap.add_argument("--duration", type=float, default=None, help="served: stream length (s)")
+    ap.add_argument("--hbm-budget-gb", type=float, default=0.0,
+                    help="served: the server's HBM admission budget (0: half the free memory)")
     ap.add_argument("--repeats", type=int, default=1, help="served: repeats of the stream and saturation runs, "
                     "served and plain interleaved")
     ap.add_argument("--contents", type=int, default=128, help="served: distinct chunks the stream draws from")
@@ -923,8 +925,10 @@ def run_served(args):
     picks = rng.integers(len(contents), size=n)
     nsat = args.saturation_chunks
     sat_picks = rng.integers(len(contents), size=nsat)
-    served_cfg = {"max_batch": args.max_batch, "max_inflight": args.max_inflight, "spin_wait": not args.no_spin}
-    plain_cfg = {"max_batch": 1, "max_inflight": 1, "spin_wait": not args.no_spin}
+    budget = int(args.hbm_budget_gb * (1 << 30)) if args.hbm_budget_gb > 0 else 0
+    served_cfg = {"max_batch": args.max_batch, "max_inflight": args.max_inflight, "spin_wait": not args.no_spin,
+                  "hbm_budget_bytes": budget}
+    plain_cfg = {"max_batch": 1, "max_inflight": 1, "spin_wait": not args.no_spin, "hbm_budget_bytes": budget}
     out = {}
     reps = {k: [] for k in ("served", "plain", "served_saturation", "plain_saturation")}
     clocks = ClockSampler(gpu_uuid(torch, 0))
