@@ -54,6 +54,8 @@ def parse_args():
         help="only launch the tensor-core kernel (resident weights), for ncu captures; prints no measurement",
     )
     ap.add_argument("--frequencies", type=int, default=None, help="override f (profiling a smaller case)")
+    ap.add_argument("--beams", type=int, default=None,
+                    help="override b (profiling: b <= 64 runs the two-unpack-group layout)")
     ap.add_argument(
         "--workload",
         choices=["chunk", "batched", "served", "wide"],
@@ -1154,10 +1156,13 @@ def main():
     if args.workload == "wide":
         run_wide(args)
         return
+    global WORKLOAD_NAME
     if args.frequencies:
         WORKLOAD["nfrequencies"] = args.frequencies
-        global WORKLOAD_NAME
         WORKLOAD_NAME = WORKLOAD_NAME.replace("f=84", f"f={args.frequencies}")
+    if args.beams:
+        WORKLOAD["nbeams"] = args.beams
+        WORKLOAD_NAME = WORKLOAD_NAME.replace("b=96", f"b={args.beams}")
     if args.profile_kernel:
         profile_kernel(args)
     elif args.impl == "reference":
