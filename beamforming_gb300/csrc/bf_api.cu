@@ -9,10 +9,8 @@
 
 #include <algorithm>
 #include <atomic>
-#include <condition_variable>
 #include <cstdlib>
 #include <cstring>
-#include <memory>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -52,23 +50,6 @@ struct DevBuf {
   }
 };
 
-// Growable pinned host buffer with a device mapping.
-struct HostBuf {
-  void *p = nullptr;
-  void *dev = nullptr;
-  size_t cap = 0;
-  cudaError_t reserve(size_t n) {
-    if (n <= cap) return cudaSuccess;
-    if (p) cudaFreeHost(p);
-    p = dev = nullptr;
-    cap = 0;
-    cudaError_t e = cudaHostAlloc(&p, n, cudaHostAllocMapped);
-    if (e == cudaSuccess) e = cudaHostGetDevicePointer(&dev, p, 0);
-    if (e == cudaSuccess) cap = n;
-    return e;
-  }
-};
-
 // One pipeline lane of the host-pointer path: a stream and the E chunk in flight on it.
 struct Lane {
   cudaStream_t s = nullptr;
@@ -89,8 +70,6 @@ struct DeviceCtx {
   DevBuf W, dig;            // tensor-core operand for non-resident calls
   DevBuf partials;          // adler32 partial sums
   DevBuf adl;               // fused adler32 sums {sum d_i, sum i d_i} of the last checked call
-  HostBuf jring;            // pinned ring for J chunks bound for a pageable J
-  cudaEvent_t jready[3] = {nullptr, nullptr, nullptr};  // a ring slot's gather has landed
 };
 
 constexpr int kMaxDevices = 64;
@@ -255,22 +234,6 @@ __global__ void __launch_bounds__(256) drain_rows(const uint8_t *__restrict__ sr
   }
 }
 
-// Copies `len` bytes at offset `off` of each of `rows` rows (`pitch` bytes
-// apart) from the device J into consecutive rows of `len` bytes at dst (a
-// pinned ring slot, through its device mapping); 16-byte loads and streaming
-// stores.  off, len, pitch and both base addresses are multiples of 16.
-__global__ void __launch_bounds__(256) gather_rows(const uint8_t *__restrict__ src, uint8_t *__restrict__ dst,
-                                                   int64_t rows, int64_t pitch, int64_t off, int64_t len) {
-  const int64_t per_row = len / 16;
-  const int64_t total = rows * per_row;
-  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
-       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    const int64_t r = i / per_row;
-    const int64_t c = 16 * (i - r * per_row);
-    __stcs(reinterpret_cast<uint4 *>(dst + r * len + c), __ldcs(reinterpret_cast<const uint4 *>(src + r * pitch + off + c)));
-  }
-}
-
 // Device address of the caller's J when it is pinned host memory that the
 // drain can write directly (16-byte aligned, rows a multiple of 16 bytes);
 // null otherwise (pageable memory: one copy at the end instead).
@@ -286,96 +249,6 @@ uint8_t *mapped_host_j(uint8_t *J, const bf_dims &d, int j_layout) {
     return nullptr;
   return static_cast<uint8_t *>(at.devicePointer);
 }
-
-// Pageable J of the host-pointer path: chunk k's J rows are gathered into slot
-// k % 3 of a pinned ring on its lane's stream, and this copier thread scatters
-// each landed slot into the caller's rows (in parallel) while later chunks
-// compute, instead of one copy of all of J at the end.
-class JScatter {
- public:
-  JScatter(int device, uint8_t *J, const HostBuf &ring, cudaEvent_t *ready, int64_t rows, int64_t pitch,
-           int64_t slot_bytes)
-      : device_(device), J_(J), ring_(static_cast<uint8_t *>(ring.p)), ready_(ready), rows_(rows), pitch_(pitch),
-        slot_(slot_bytes) {
-    th_ = std::thread([this] { run(); });
-  }
-  ~JScatter() { finish(); }
-  // Blocks until slot k % 3 is free (chunk k - 3 scattered); false on a copier error.
-  bool wait_slot(int64_t k) {
-    std::unique_lock<std::mutex> lk(m_);
-    cv_.wait(lk, [&] { return done_ >= k - 2 || err_ != cudaSuccess; });
-    return err_ == cudaSuccess;
-  }
-  // Chunk k (gather enqueued and its event recorded): byte `off` of each row,
-  // `len` bytes; the slot holds the rows back to back.
-  void push(int64_t off, int64_t len) {
-    {
-      std::lock_guard<std::mutex> lk(m_);
-      chunks_.push_back({off, len});
-    }
-    cv_.notify_all();
-  }
-  // Waits for every pushed chunk to be scattered; the first CUDA error seen.
-  cudaError_t finish() {
-    {
-      std::lock_guard<std::mutex> lk(m_);
-      stop_ = true;
-    }
-    cv_.notify_all();
-    if (th_.joinable()) th_.join();
-    return err_;
-  }
-
- private:
-  void run() {
-    cudaSetDevice(device_);
-    const unsigned hw = std::max(2u, std::thread::hardware_concurrency());
-    const int64_t nworkers = std::min<int64_t>(16, hw - 1);
-    for (int64_t k = 0;; ++k) {
-      std::pair<int64_t, int64_t> ch;
-      {
-        std::unique_lock<std::mutex> lk(m_);
-        cv_.wait(lk, [&] { return static_cast<int64_t>(chunks_.size()) > k || stop_; });
-        if (static_cast<int64_t>(chunks_.size()) <= k) return;  // stopped with nothing more pushed
-        ch = chunks_[static_cast<size_t>(k)];
-      }
-      const cudaError_t e = cudaEventSynchronize(ready_[k % 3]);
-      if (e != cudaSuccess) {
-        std::lock_guard<std::mutex> lk(m_);
-        err_ = e;
-        cv_.notify_all();
-        return;
-      }
-      const uint8_t *slot = ring_ + (k % 3) * slot_;
-      const int64_t off = ch.first, len = ch.second, per = (rows_ + nworkers - 1) / nworkers;
-      std::vector<std::thread> ws;
-      for (int64_t w = 0; w < nworkers && w * per < rows_; ++w)
-        ws.emplace_back([=] {
-          for (int64_t r = w * per; r < std::min(rows_, (w + 1) * per); ++r)
-            std::memcpy(J_ + r * pitch_ + off, slot + r * len, static_cast<size_t>(len));
-        });
-      for (auto &t : ws) t.join();
-      {
-        std::lock_guard<std::mutex> lk(m_);
-        done_ = k + 1;
-      }
-      cv_.notify_all();
-    }
-  }
-
-  int device_;
-  uint8_t *J_;
-  uint8_t *ring_;
-  cudaEvent_t *ready_;
-  int64_t rows_, pitch_, slot_;
-  std::thread th_;
-  std::mutex m_;
-  std::condition_variable cv_;
-  std::vector<std::pair<int64_t, int64_t>> chunks_;
-  int64_t done_ = 0;
-  bool stop_ = false;
-  cudaError_t err_ = cudaSuccess;
-};
 
 // Host-pointer pass pipelined over time chunks: E[t0..t1][f][d][p] is
 // contiguous, so each chunk goes in with one copy on one of kLanes streams and
@@ -433,17 +306,6 @@ int run_host_pipelined(DeviceCtx &c, const bf_dims &d, uint8_t *J, const uint8_t
   const int64_t jrows = j_layout == kJ2 ? d.nbeams * d.nfrequencies : d.nbeams * d.nfrequencies * P;
   const int64_t jpitch = j_layout == kJ2 ? T * P : T;
   const int64_t jscale = j_layout == kJ2 ? P : 1;  // bytes per time in a row
-  // pageable J with 16-byte row segments: through the pinned ring, chunk by chunk
-  const int64_t slot_bytes = (jrows * tc * jscale + 255) / 256 * 256;
-  std::unique_ptr<JScatter> scatter;
-  if (!jmap && (jpitch % 16) == 0 && ((T * jscale) % 16) == 0 && c.jring.reserve(3 * slot_bytes) == cudaSuccess) {
-    for (cudaEvent_t &ev : c.jready)
-      if (!ev) BF_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-    int dev = 0;
-    BF_TRY(cudaGetDevice(&dev));
-    scatter = std::make_unique<JScatter>(dev, J, c.jring, c.jready, jrows, jpitch, slot_bytes);
-  }
-  (void)cudaGetLastError();  // a failed ring allocation leaves the end-of-pass copy in use
   for (int64_t t0 = 0, k = 0; t0 < T; t0 += tc, ++k) {
     Lane &l = c.lanes[k % kLanes];
     const int64_t nt = std::min(tc, T - t0);
@@ -461,26 +323,13 @@ int run_host_pipelined(DeviceCtx &c, const bf_dims &d, uint8_t *J, const uint8_t
       const int grid = 2 * std::max(1, num_sms_api());
       drain_rows<<<grid, 256, 0, l.s>>>(c.J.as<uint8_t>(), jmap, jrows, jpitch, t0 * jscale, nt * jscale);
       BF_TRY(cudaGetLastError());
-    } else if (scatter) {
-      if (!scatter->wait_slot(k)) return to_status(scatter->finish());
-      const int64_t len = nt * jscale;
-      const int grid = 2 * std::max(1, num_sms_api());
-      uint8_t *slot = static_cast<uint8_t *>(c.jring.dev) + (k % 3) * slot_bytes;
-      gather_rows<<<grid, 256, 0, l.s>>>(c.J.as<uint8_t>(), slot, jrows, jpitch, t0 * jscale, len);
-      BF_TRY(cudaGetLastError());
-      BF_TRY(cudaEventRecord(c.jready[k % 3], l.s));
-      scatter->push(t0 * jscale, len);
     }
   }
   for (int i = 1; i < kLanes; ++i) {
     BF_TRY(cudaEventRecord(c.lanes[i].done, c.lanes[i].s));
     BF_TRY(cudaStreamWaitEvent(l0.s, c.lanes[i].done, 0));
   }
-  if (scatter) {
-    BF_TRY(scatter->finish());
-  } else if (!jmap) {
-    BF_TRY(cudaMemcpyAsync(J, c.J.p, jsize(d), cudaMemcpyDeviceToHost, l0.s));
-  }
+  if (!jmap) BF_TRY(cudaMemcpyAsync(J, c.J.p, jsize(d), cudaMemcpyDeviceToHost, l0.s));
   BF_TRY(cudaStreamSynchronize(l0.s));
   return read_and_clear_err(c, caller);
 }
