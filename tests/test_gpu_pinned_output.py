@@ -74,3 +74,37 @@ def test_pinned_J_with_unaligned_rows_falls_back(bflib, cuda, oracle, monkeypatc
     J[:] = 0x5A
     bflib.form_beams_ex(d, J, E, A, G)
     np.testing.assert_array_equal(J, _oracle_J(oracle, d, E, A, G, "linear"))
+
+
+@pytest.mark.parametrize("kernel", ["tensor", "simt"])
+@pytest.mark.parametrize("T", [1024, 1040])
+@pytest.mark.parametrize("j_layout", ["linear", "j2"])
+def test_pageable_J_pipelined(bflib, cuda, oracle, monkeypatch, j_layout, T, kernel):
+    """J in pageable memory (the drop-in case: the reference's main passes
+    std::vector storage) through the chunked host pipeline: J leaves in one
+    copy after the last chunk; the bytes equal the oracle's, twice in a row,
+    including a 16-time last chunk."""
+    monkeypatch.setenv("BF_HOST_CHUNK_BYTES", str(256 * 4 * 512 * 2))
+    d = bflib.Dims(T, 4, 512, 2, 96)
+    E, A, G = bflib.seeded_host_inputs(d, T + 7 + (1 if j_layout == "j2" else 0))
+    expect = _oracle_J(oracle, d, E, A, G, j_layout)
+    bflib.set_kernel(kernel)
+    try:
+        for _ in range(2):
+            J = np.full(d.jsize, 0x5A, np.uint8)  # pageable
+            bflib.form_beams_layout(d, J, E, A, G, j_layout=j_layout)
+            assert bflib.last_kernel() == kernel
+            np.testing.assert_array_equal(J, expect)
+    finally:
+        bflib.set_kernel("auto")
+
+
+def test_pageable_J_with_checksum(bflib, cuda, oracle, monkeypatch):
+    monkeypatch.setenv("BF_HOST_CHUNK_BYTES", str(256 * 4 * 512 * 2))
+    d = bflib.Dims(1024, 4, 512, 2, 96)
+    E, A, G = bflib.seeded_host_inputs(d, 41)
+    J = np.zeros(d.jsize, np.uint8)
+    got = bflib.form_beams_adler(d, J, E, A, G)
+    expect = _oracle_J(oracle, d, E, A, G, "linear")
+    np.testing.assert_array_equal(J, expect)
+    assert got == zlib.adler32(expect.tobytes())
