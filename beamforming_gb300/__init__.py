@@ -175,7 +175,7 @@ def lib() -> ctypes.CDLL:
         L.bf_batch_create.argtypes = [ctypes.POINTER(vp), ctypes.c_void_p, ctypes.c_int, vp]
         L.bf_batch_run.argtypes = [vp, vp]
         L.bf_batch_info.argtypes = [vp] + [ctypes.POINTER(ctypes.c_int)] * 4 + [ctypes.POINTER(ctypes.c_float)]
-        L.bf_batch_shape.argtypes = [vp] + [ctypes.POINTER(ctypes.c_int)] * 6
+        L.bf_batch_shape.argtypes = [vp] + [ctypes.POINTER(ctypes.c_int)] * 7
         L.bf_batch_destroy.argtypes = [vp]
         L.bf_server_create.argtypes = [ctypes.POINTER(vp), vp, ctypes.POINTER(_ServerConfig)]
         L.bf_server_submit.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int64, u8p, ctypes.c_int, u8p,
@@ -511,9 +511,9 @@ class Batch:
         info = {"ntiles": nt.value, "order": ("given", "largest_first")[order.value], "wslots": ws.value,
                 "raw_slots": raw.value, "tuned_ms": ms.value}
         n = ctypes.c_int()
-        arrs = [(ctypes.c_int * 2)() for _ in range(5)]
+        arrs = [(ctypes.c_int * 3)() for _ in range(6)]
         _check(lib().bf_batch_shape(self._h, ctypes.byref(n), *arrs), "bf_batch_shape")
-        names = ("problems", "tiles", "max_nb_pass", "stages", "unpack_groups")
+        names = ("problems", "tiles", "max_nb_pass", "stages", "unpack_groups", "ctas_per_sm")
         info["launches"] = [{k: a[i] for k, a in zip(names, arrs)} for i in range(n.value)]
         return info
 

@@ -5,12 +5,14 @@
 // shape -- ntimes and nbeams may all differ; ndishes is shared -- and the
 // tensor-core kernel walks one tile list that spans all of them.  At creation
 // an autotuner times a few schedules on the real buffers and keeps the
-// fastest: the tile shape (one launch for every problem, or the problems whose
-// beam passes are at most 64 beams wide in a launch of their own, where four
-// or more unpacked stages fit in tensor memory beside narrower accumulators
-// and two unpack groups keep the tensor core fed), the tile order, and the
-// shared-memory ring plan.  The chosen launches are captured in a CUDA graph,
-// and bf_batch_run() replays it.
+// fastest: the tile shape, the tile order and the shared-memory ring plan.
+// The tile shape groups the problems by beam-pass width into up to three
+// launches: wide passes (more than 64 beams), narrow ones (at most 64: four or
+// more unpacked stages fit in tensor memory beside the narrower accumulators,
+// and two unpack groups keep the tensor core fed) and the narrowest (at most
+// 16: two CTAs share each SM).  A launch takes the layout of its widest pass,
+// so each cut between classes is kept only when timing says so.  The chosen
+// launches are captured in a CUDA graph, and bf_batch_run() replays it.
 #include "bf_internal.h"
 
 #include <algorithm>
@@ -20,8 +22,9 @@
 namespace {
 // One grouped launch of a batch: a range of the device problem table.
 struct BatchLaunch {
-  int first = 0, nprob = 0, ntiles = 0, max_nb_pass = 0, stages = 0, groups = 0;
+  int first = 0, nprob = 0, ntiles = 0, max_nb_pass = 0, stages = 0, groups = 0, ctas_per_sm = 0;
 };
+constexpr int kMaxLaunches = 3;  // one per pass-width class
 }  // namespace
 
 struct bf_batch {
@@ -33,9 +36,9 @@ struct bf_batch {
   bf::TcProblem *table = nullptr;  // device copy, launch order
   bf::TcRingPlan plan;
   int order = 0;                   // chosen tile order (0: as given, 1: largest problem first)
-  int split = 0;                   // chosen tile shape (0: one launch, 1: narrow passes apart)
+  int cuts = 0;                    // chosen tile shape: bit c set = classes c and c + 1 in separate launches
   int nlaunch = 0;
-  BatchLaunch launches[2];
+  BatchLaunch launches[kMaxLaunches];
   float tuned_ms = 0.0f;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -62,20 +65,26 @@ int status_of(cudaError_t e) {
 struct Schedule {
   std::vector<TcProblem> table;
   int nlaunch = 0;
-  BatchLaunch launches[2];
+  BatchLaunch launches[kMaxLaunches];
 };
 
-// Problems in `order`, split by pass width when `split` (passes wider than
-// kNarrowPass first); empty classes are dropped.
-Schedule schedule_of(const std::vector<TcProblem> &probs, const std::vector<int> &order, bool split) {
+// Pass-width class of a problem: 0 wide, 1 narrow (<= kNarrowPass beams),
+// 2 narrowest (<= kHalfPass beams).
+int class_of(const TcProblem &P) { return P.nb_pass <= kHalfPass ? 2 : P.nb_pass <= kNarrowPass ? 1 : 0; }
+
+// Launch of class c under `cuts`: the number of cuts below it.
+int launch_of(int cls, int cuts) { return (cls >= 1 && (cuts & 1)) + (cls >= 2 && (cuts & 2)); }
+
+// Problems in `order`, one launch per group of classes that `cuts` keeps
+// together (wider classes first); empty launches are dropped.
+Schedule schedule_of(const std::vector<TcProblem> &probs, const std::vector<int> &order, int cuts) {
   Schedule sc;
-  for (int cls = 0; cls < (split ? 2 : 1); ++cls) {
+  for (int l = 0; l < kMaxLaunches; ++l) {
     BatchLaunch L;
     L.first = static_cast<int>(sc.table.size());
     int64_t begin = 0;
     for (int i : order) {
-      const bool narrow = probs[i].nb_pass <= kNarrowPass;
-      if (split && narrow != (cls == 1)) continue;
+      if (launch_of(class_of(probs[i]), cuts) != l) continue;
       TcProblem P = probs[i];
       P.tile_begin = static_cast<int>(begin);
       begin += tc_problem_tiles(P);
@@ -108,8 +117,8 @@ int bf_batch_create(bf_batch **out, const bf_problem *problems, int nproblems, b
   *out = nullptr;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   int64_t D = -1;
-  int max_nb = 0, min_nb = 1 << 30;
   std::vector<TcProblem> probs(static_cast<size_t>(nproblems));
+  bool present[3] = {false, false, false};
   for (int i = 0; i < nproblems; ++i) {
     const bf_problem &q = problems[i];
     if (!q.weights || !q.E || !q.J || q.ntimes <= 0) return BF_ERR_INVALID_ARGUMENT;
@@ -119,8 +128,7 @@ int bf_batch_create(bf_batch **out, const bf_problem *problems, int nproblems, b
     if (w.D != D || !tc_supported(d)) return BF_ERR_UNSUPPORTED;
     if ((reinterpret_cast<uintptr_t>(q.E) | reinterpret_cast<uintptr_t>(q.J)) & 15u) return BF_ERR_UNSUPPORTED;
     BF_TRY(tc_make_problem(probs[i], w, q.ntimes, q.J, q.E, 0));
-    max_nb = std::max(max_nb, w.nb_pass);
-    min_nb = std::min(min_nb, w.nb_pass);
+    present[class_of(probs[i])] = true;
   }
   int *err = nullptr;
   int st = device_error_word(&err);
@@ -138,7 +146,7 @@ int bf_batch_create(bf_batch **out, const bf_problem *problems, int nproblems, b
 
   // Autotune: tile shape x tile order x ring plan, each timed on the real
   // buffers (every candidate writes the same J, so the outputs are valid
-  // afterwards).  Splitting only applies when both pass classes are present.
+  // afterwards).  A cut is tried only where classes sit on both sides of it.
   std::vector<int> given(static_cast<size_t>(nproblems));
   std::iota(given.begin(), given.end(), 0);
   std::vector<int> largest = given;
@@ -146,7 +154,7 @@ int bf_batch_create(bf_batch **out, const bf_problem *problems, int nproblems, b
     return tc_problem_tiles(probs[x]) > tc_problem_tiles(probs[y]);
   });
   const std::vector<int> *orders[2] = {&given, &largest};
-  const int nsplit = (min_nb <= kNarrowPass && max_nb > kNarrowPass) ? 2 : 1;
+  const bool cut_ok[2] = {present[0] && (present[1] || present[2]), present[2] && (present[0] || present[1])};
   TcRingPlan plans[3];
   plans[1].wslots = 4;
   plans[1].raw = 8;
@@ -157,9 +165,10 @@ int bf_batch_create(bf_batch **out, const bf_problem *problems, int nproblems, b
   cudaEventCreate(&e1);
   float best = -1.0f;
   st = BF_OK;
-  for (int sp = 0; sp < nsplit && st == BF_OK; ++sp) {
+  for (int cuts = 0; cuts < 4 && st == BF_OK; ++cuts) {
+    if (((cuts & 1) && !cut_ok[0]) || ((cuts & 2) && !cut_ok[1])) continue;
     for (int o = 0; o < 2 && st == BF_OK; ++o) {
-      const Schedule sc = schedule_of(probs, *orders[o], sp == 1);
+      const Schedule sc = schedule_of(probs, *orders[o], cuts);
       cudaError_t e = cudaMemcpyAsync(b->table, sc.table.data(), sizeof(TcProblem) * sc.table.size(),
                                       cudaMemcpyHostToDevice, s);
       for (int pl = 0; pl < 3 && e == cudaSuccess; ++pl) {
@@ -173,7 +182,7 @@ int bf_batch_create(bf_batch **out, const bf_problem *problems, int nproblems, b
         if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
         if (e == cudaSuccess && (best < 0.0f || ms < best)) {
           best = ms;
-          b->split = sp;
+          b->cuts = cuts;
           b->order = o;
           b->plan = plans[pl];
         }
@@ -184,15 +193,15 @@ int bf_batch_create(bf_batch **out, const bf_problem *problems, int nproblems, b
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (st == BF_OK) {
-    const Schedule sc = schedule_of(probs, *orders[b->order], b->split == 1);
+    const Schedule sc = schedule_of(probs, *orders[b->order], b->cuts);
     b->tuned_ms = best / 3.0f;
     b->nlaunch = sc.nlaunch;
     b->ntiles = 0;
     for (int i = 0; i < sc.nlaunch; ++i) {
       b->launches[i] = sc.launches[i];
       b->ntiles += sc.launches[i].ntiles;
-      if (tc_launch_shape(D, b->launches[i].max_nb_pass, b->plan, &b->launches[i].stages, &b->launches[i].groups) !=
-          cudaSuccess)
+      BatchLaunch &L = b->launches[i];
+      if (tc_launch_shape(D, L.max_nb_pass, b->plan, &L.stages, &L.groups, &L.ctas_per_sm) != cudaSuccess)
         st = BF_ERR_UNSUPPORTED;
     }
     cudaError_t e = cudaMemcpyAsync(b->table, sc.table.data(), sizeof(TcProblem) * sc.table.size(),
@@ -235,7 +244,7 @@ int bf_batch_info(const bf_batch *b, int *ntiles, int *order, int *wslots, int *
 }
 
 int bf_batch_shape(const bf_batch *b, int *nlaunches, int *nproblems, int *ntiles, int *max_nb_pass, int *stages,
-                   int *unpack_groups) {
+                   int *unpack_groups, int *ctas_per_sm) {
   if (!b || !nlaunches) return BF_ERR_INVALID_ARGUMENT;
   *nlaunches = b->nlaunch;
   for (int i = 0; i < b->nlaunch; ++i) {
@@ -245,6 +254,7 @@ int bf_batch_shape(const bf_batch *b, int *nlaunches, int *nproblems, int *ntile
     if (max_nb_pass) max_nb_pass[i] = L.max_nb_pass;
     if (stages) stages[i] = L.stages;
     if (unpack_groups) unpack_groups[i] = L.groups;
+    if (ctas_per_sm) ctas_per_sm[i] = L.ctas_per_sm;
   }
   return BF_OK;
 }

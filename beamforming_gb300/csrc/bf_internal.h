@@ -168,12 +168,17 @@ int tc_stages_per_tile(int64_t D);
 cudaError_t launch_tc_grouped(const TcProblem *table, int nprob, int ntiles, int64_t D, int max_nb_pass,
                               const TcRingPlan &plan, int *err, cudaStream_t s);
 
-// TMEM stages and unpack groups a grouped launch with these sizes would use.
-cudaError_t tc_launch_shape(int64_t D, int max_nb_pass, const TcRingPlan &plan, int *stages, int *groups);
+// TMEM stages, unpack groups and CTAs per SM of a grouped launch with these sizes.
+cudaError_t tc_launch_shape(int64_t D, int max_nb_pass, const TcRingPlan &plan, int *stages, int *groups,
+                            int *ctas_per_sm);
 
-// Beam passes of at most this many beams leave room for four or more unpacked
-// stages in TMEM, and so for two unpack groups.
+// Beam passes of at most kNarrowPass beams leave room for four or more
+// unpacked stages in TMEM, and so for two unpack groups.  Passes of at most
+// kHalfPass beams fit a CTA with half the SM's TMEM and shared memory, so two
+// CTAs share each SM (measured 1.3x on b = 16 passes; at b = 32 the two TMEM
+// stages a half CTA keeps lose 5% against six stages and two unpack groups).
 constexpr int kNarrowPass = 64;
+constexpr int kHalfPass = 16;
 
 // Failure-path test hook: nonzero makes the producer of later tensor-core
 // launches issue nothing, so the kernel's bounded waits expire.

@@ -90,6 +90,12 @@ static_assert(kSub == 2, "mma_ts_stage8 issues the eight MMAs of two W boxes");
 constexpr int kRawBox = kTT * kKC;      // raw E per box: 64 times x 64 dishes x 2 pol
 constexpr int kRawBytes = kSub * kRawBox;
 constexpr int kAccCols = 256;           // TMEM column offset of the second accumulator
+// Beam passes of at most kHalfPass beams run the half-SM layout: 4 epilogue
+// warps, 256 TMEM columns (second accumulator at column 128) and at most
+// kSmemLimitHalf bytes of shared memory, so that two CTAs share each SM and
+// each SM has two MMA issuers, two unpack chains and two epilogues.
+constexpr int kAccColsHalf = 128;
+constexpr int kSmemLimitHalf = 115712;  // half of the SM's 228 KiB less the 1 KiB each block reserves
 constexpr int kStageCols = kStageK / 4;  // TMEM columns per unpacked stage
 constexpr int kSmemLimit = 232448;      // 227 KiB opt-in per block
 constexpr int kMaxStages = 8;
@@ -120,6 +126,7 @@ struct TcParams {
   int raw;                  // raw E slots in smem
   int test_stall;           // nonzero: the producers issue nothing (failure-path test)
   int groups;               // unpack groups (2: with the W forwarder; needs stages >= 4)
+  int half;                 // nonzero: the half-SM layout (two CTAs per SM)
   int *err;
 };
 
@@ -236,9 +243,9 @@ __host__ __device__ inline SmemPlan smem_plan(int stages, int wslots, int raw, i
 }
 
 // TMEM column of unpacked stage i: the columns left over after the two accumulators.
-__host__ __device__ inline uint32_t stage_col(int i, int ncols, int per_half) {
+__host__ __device__ inline uint32_t stage_col(int i, int ncols, int per_half, int acc_cols) {
   return i < per_half ? static_cast<uint32_t>(ncols + kStageCols * i)
-                      : static_cast<uint32_t>(kAccCols + ncols + kStageCols * (i - per_half));
+                      : static_cast<uint32_t>(acc_cols + ncols + kStageCols * (i - per_half));
 }
 
 // Position in a ring of n slots: slot index and the parity of the pass over the ring.
@@ -272,10 +279,11 @@ __device__ __forceinline__ uint32_t sw128_offset(uint32_t r, uint32_t j) {
   return (r >> 3) * 1024u + (r & 7u) * 128u + ((j ^ (r & 7u)) << 4);
 }
 
-template <bool kGrouped, bool kJ2, int kEpiW, bool kAdler, int kGroups>
-__global__ void __launch_bounds__(Roles<kEpiW, kGroups>::kThreads, 1)
+template <bool kGrouped, bool kJ2, int kEpiW, bool kAdler, int kGroups, bool kHalf>
+__global__ void __launch_bounds__(Roles<kEpiW, kGroups>::kThreads, kHalf ? 2 : 1)
     bf_form_beams_tc(const __grid_constant__ TcParams p) {
   using RL = Roles<kEpiW, kGroups>;
+  constexpr int kAcc = kHalf ? kAccColsHalf : kAccCols;  // TMEM column of the second accumulator
   constexpr int kEpiThreads = RL::kEpiThreads, kEpiParts = RL::kEpiParts, kEProdWarp = RL::kEProdWarp;
   constexpr int kMmaWarp = RL::kMmaWarp, kWProdWarp = RL::kWProdWarp, kUnpackWarp0 = RL::kUnpackWarp0;
   constexpr int kUnpackGroups = RL::kUnpackGroups;
@@ -303,7 +311,7 @@ __global__ void __launch_bounds__(Roles<kEpiW, kGroups>::kThreads, 1)
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
   const int ncols = 2 * p.max_nb_pass;                 // accumulator columns reserved (largest GEMM N)
-  const int per_half = (kAccCols - ncols) / kStageCols;  // unpacked stages beside each accumulator
+  const int per_half = (kAcc - ncols) / kStageCols;  // unpacked stages beside each accumulator
 
   if (threadIdx.x == 0) {
     for (int r = 0; r < R; ++r) {
@@ -336,7 +344,7 @@ __global__ void __launch_bounds__(Roles<kEpiW, kGroups>::kThreads, 1)
   }
   fence_proxy_async_smem();
   if (warp == kMmaWarp) {
-    tmem_alloc(smem_u32(tmem_holder), 2 * kAccCols);
+    tmem_alloc(smem_u32(tmem_holder), 2 * kAcc);
     tmem_relinquish();
   }
   if (!kGrouped && warp == kEProdWarp && lane == 0) {
@@ -477,7 +485,7 @@ __global__ void __launch_bounds__(Roles<kEpiW, kGroups>::kThreads, 1)
         const int ds = static_cast<int>(dr.idx);
         if (!mbar_wait(d_full(ds), dr.phase, err, kDevTimeoutFull)) break;
         tc_fence_after();
-        const uint32_t d_tmem = tmem_base + ab * kAccCols;
+        const uint32_t d_tmem = tmem_base + ab * kAcc;
         // the offset MMA starts the accumulator at -8 sum_k W[n][k] / 512
         mma_f8f6f4(d_tmem, a_const, smem_desc_sw32(smem_u32(sD + ds * sp.dbytes)), idesc, 0u);
         mma_commit(d_empty(ds));
@@ -491,7 +499,7 @@ __global__ void __launch_bounds__(Roles<kEpiW, kGroups>::kThreads, 1)
             break;
           }
           tc_fence_after();
-          const uint32_t a_tmem = tmem_base + stage_col(s, ncols, per_half);
+          const uint32_t a_tmem = tmem_base + stage_col(s, ncols, per_half, kAcc);
           const uint64_t b_desc = w_desc0 + static_cast<uint64_t>((sw * sp.wbytes) >> 4);
           mma_ts_stage8(d_tmem, a_tmem, b_desc, b_desc + static_cast<uint64_t>(wbox >> 4), idesc);
           mma_commit(empty(s));  // also frees the W slot: the unpack passes it on
@@ -554,7 +562,7 @@ __global__ void __launch_bounds__(Roles<kEpiW, kGroups>::kThreads, 1)
           ok = false;  // the warp leaves together
           break;
         }
-        const uint32_t col = tmem_base + lane_addr + stage_col(s, ncols, per_half);
+        const uint32_t col = tmem_base + lane_addr + stage_col(s, ncols, per_half, kAcc);
         // the whole stage goes to registers first, so that only the tensor-memory
         // stores wait for the tensor core to release the stage
         uint32_t out[kSub][32];
@@ -643,7 +651,7 @@ __global__ void __launch_bounds__(Roles<kEpiW, kGroups>::kThreads, 1)
       const bool wide = __ldg(P.gwide + f) != 0;
       if (!__all_sync(0xffffffffu, mbar_wait(accfull(ab), aph, err, kDevTimeoutAccFull))) break;
       tc_fence_after();
-      const uint32_t acc_addr = tmem_base + ab * kAccCols + lane_addr;
+      const uint32_t acc_addr = tmem_base + ab * kAcc + lane_addr;
       // A 4x4 byte transpose among 4 lanes turns "4 beams of one row" into "4
       // rows of one beam" in each lane.  Jlinear (arraysizes.hxx:92): the 4 lanes
       // of equal polarization and consecutive times (lane bits 1 and 2) exchange,
@@ -774,7 +782,7 @@ __global__ void __launch_bounds__(Roles<kEpiW, kGroups>::kThreads, 1)
   __syncthreads();
   if (warp == kMmaWarp) {
     tc_fence_after();
-    tmem_dealloc(tmem_base, 2 * kAccCols);
+    tmem_dealloc(tmem_base, 2 * kAcc);
   }
 }
 
@@ -990,7 +998,10 @@ static cudaError_t make_problem(TcProblem &P, const TcWeights &w, int64_t T, uin
 static cudaError_t plan_launch(TcParams &p, int max_nb_pass, const TcRingPlan &plan, int *smem_bytes) {
   // unpacked stages live in the TMEM columns beside the two accumulators; raw E
   // slots take the shared memory the W slots leave
-  const int per_half = (kAccCols - 2 * max_nb_pass) / kStageCols;
+  const bool half = max_nb_pass <= kHalfPass;
+  const int acc_cols = half ? kAccColsHalf : kAccCols;
+  const int smem_limit = half ? kSmemLimitHalf : kSmemLimit;
+  const int per_half = (acc_cols - 2 * max_nb_pass) / kStageCols;
   const int stages = std::min(kMaxStages, 2 * per_half);
   if (stages < 2) return cudaErrorInvalidValue;
   // shared memory: W slots first (their loads gate the MMA), then raw E slots
@@ -998,10 +1009,10 @@ static cudaError_t plan_launch(TcParams &p, int max_nb_pass, const TcRingPlan &p
   const int want_r = plan.raw > 0 ? plan.raw : g_plan_raw;
   int wslots = want_w > 0 ? want_w : kMaxWSlots;
   int raw = want_r > 0 ? want_r : kMinRaw;
-  while (wslots > 2 && smem_plan(stages, wslots, raw, max_nb_pass).total + 1024 > kSmemLimit) --wslots;
-  while (raw < kMaxRaw && smem_plan(stages, wslots, raw + 1, max_nb_pass).total + 1024 <= kSmemLimit && want_r <= 0)
+  while (wslots > 2 && smem_plan(stages, wslots, raw, max_nb_pass).total + 1024 > smem_limit) --wslots;
+  while (raw < kMaxRaw && smem_plan(stages, wslots, raw + 1, max_nb_pass).total + 1024 <= smem_limit && want_r <= 0)
     ++raw;
-  while (raw > 2 && smem_plan(stages, wslots, raw, max_nb_pass).total + 1024 > kSmemLimit) --raw;
+  while (raw > 2 && smem_plan(stages, wslots, raw, max_nb_pass).total + 1024 > smem_limit) --raw;
   // Four or more unpacked stages: two unpack groups and the W forwarder, whose
   // W slots are reused straight after the tensor core's release (this needs
   // SW <= 2 S, true for every plan here).  Otherwise one group, which hands W
@@ -1014,34 +1025,42 @@ static cudaError_t plan_launch(TcParams &p, int max_nb_pass, const TcRingPlan &p
   p.wslots = wslots;
   p.raw = raw;
   p.groups = groups;
+  p.half = half ? 1 : 0;
   p.test_stall = g_test_stall;
   *smem_bytes = smem_plan(st, wslots, raw, max_nb_pass).total + 1024;
-  return *smem_bytes > kSmemLimit ? cudaErrorInvalidValue : cudaSuccess;
+  return *smem_bytes > smem_limit ? cudaErrorInvalidValue : cudaSuccess;
 }
 
-template <bool kGrouped, bool kJ2, int kEpiW, bool kAdler, int kGroups>
+template <bool kGrouped, bool kJ2, int kEpiW, bool kAdler, int kGroups, bool kHalf>
 static cudaError_t launch_inst(const TcParams &p, int smem_bytes, cudaStream_t s) {
+  auto kern = bf_form_beams_tc<kGrouped, kJ2, kEpiW, kAdler, kGroups, kHalf>;
   static std::atomic<bool> attr_set{false};
   if (!attr_set.load()) {
-    const cudaError_t e = cudaFuncSetAttribute(bf_form_beams_tc<kGrouped, kJ2, kEpiW, kAdler, kGroups>,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         kHalf ? kSmemLimitHalf : kSmemLimit);
+    // two half-SM blocks per SM need the whole shared-memory carveout
+    if (e == cudaSuccess && kHalf)
+      e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
     if (e != cudaSuccess) return e;
     attr_set.store(true);
   }
-  const int grid = std::min(p.ntiles, num_sms());
+  const int grid = std::min(p.ntiles, (kHalf ? 2 : 1) * num_sms());
   if (grid <= 0) return cudaSuccess;
-  bf_form_beams_tc<kGrouped, kJ2, kEpiW, kAdler, kGroups><<<grid, Roles<kEpiW, kGroups>::kThreads, smem_bytes, s>>>(p);
+  kern<<<grid, Roles<kEpiW, kGroups>::kThreads, smem_bytes, s>>>(p);
   return cudaGetLastError();
 }
 
-// Warp layout of a launch: two unpack groups (with the forwarder) beside eight
-// epilogue warps; one group beside twelve epilogue warps up to 4 K stages per
-// tile (the epilogue paces short tiles) or eight for deeper tiles.
+// Warp layout of a launch: passes of at most kHalfPass beams run two CTAs per
+// SM of four epilogue warps and one unpack group each; otherwise two unpack
+// groups (with the forwarder) beside eight epilogue warps; one group beside
+// twelve epilogue warps up to 4 K stages per tile (the epilogue paces short
+// tiles) or eight for deeper tiles.
 template <bool kGrouped, bool kJ2, bool kAdler>
 static cudaError_t launch_layout(const TcParams &p, int smem_bytes, cudaStream_t s) {
-  if (p.groups == 2) return launch_inst<kGrouped, kJ2, 8, kAdler, 2>(p, smem_bytes, s);
-  return p.nk <= 4 ? launch_inst<kGrouped, kJ2, 12, kAdler, 1>(p, smem_bytes, s)
-                   : launch_inst<kGrouped, kJ2, 8, kAdler, 1>(p, smem_bytes, s);
+  if (p.half) return launch_inst<kGrouped, kJ2, 4, kAdler, 1, true>(p, smem_bytes, s);
+  if (p.groups == 2) return launch_inst<kGrouped, kJ2, 8, kAdler, 2, false>(p, smem_bytes, s);
+  return p.nk <= 4 ? launch_inst<kGrouped, kJ2, 12, kAdler, 1, false>(p, smem_bytes, s)
+                   : launch_inst<kGrouped, kJ2, 8, kAdler, 1, false>(p, smem_bytes, s);
 }
 
 template <bool kJ2, bool kAdler>
@@ -1071,7 +1090,8 @@ int64_t tc_problem_tiles(const TcProblem &P) { return static_cast<int64_t>(P.ntt
 
 int tc_stages_per_tile(int64_t D) { return static_cast<int>((D + kStageK / 2 - 1) / (kStageK / 2)); }
 
-cudaError_t tc_launch_shape(int64_t D, int max_nb_pass, const TcRingPlan &plan, int *stages, int *groups) {
+cudaError_t tc_launch_shape(int64_t D, int max_nb_pass, const TcRingPlan &plan, int *stages, int *groups,
+                            int *ctas_per_sm) {
   TcParams p{};
   p.nk = tc_stages_per_tile(D);
   int smem_bytes = 0;
@@ -1079,6 +1099,7 @@ cudaError_t tc_launch_shape(int64_t D, int max_nb_pass, const TcRingPlan &plan, 
   if (e != cudaSuccess) return e;
   *stages = p.stages;
   *groups = p.groups;
+  *ctas_per_sm = p.half ? 2 : 1;
   return cudaSuccess;
 }
 

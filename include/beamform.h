@@ -179,12 +179,13 @@ BF_API int bf_batch_run(bf_batch *batch, bf_stream_t stream);
  * problem first), ring plan (0 = default) and the tuned time of one run. */
 BF_API int bf_batch_info(const bf_batch *batch, int *ntiles, int *order, int *wslots, int *raw, float *tuned_ms);
 
-/* The tile shape the autotuner chose: the number of launches (1 or 2) and,
- * per launch (arrays of at least 2 entries, any of them may be NULL), its
- * problems, tiles, widest beam pass, unpacked stages in tensor memory and
- * unpack warp groups.  No counterpart in the reference. */
+/* The tile shape the autotuner chose: the number of launches (1 to 3) and,
+ * per launch (arrays of at least 3 entries, any of them may be NULL), its
+ * problems, tiles, widest beam pass, unpacked stages in tensor memory, unpack
+ * warp groups and CTAs per SM (2 when no pass is wider than 16 beams).  No
+ * counterpart in the reference. */
 BF_API int bf_batch_shape(const bf_batch *batch, int *nlaunches, int *nproblems, int *ntiles, int *max_nb_pass,
-                          int *stages, int *unpack_groups);
+                          int *stages, int *unpack_groups, int *ctas_per_sm);
 
 BF_API int bf_batch_destroy(bf_batch *batch);
 

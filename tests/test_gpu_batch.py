@@ -25,6 +25,18 @@ def _oracle(oracle, d, E, A, G):
     return oracle.form_beams(oracle.Dims(d.ntimes, d.nfrequencies, d.ndishes, 2, d.nbeams), E, A, G)
 
 
+def _check_layout(L):
+    """A launch's layout follows its widest pass: at most 16 beams two CTAs per
+    SM (two TMEM stages each); at most 64 four or more stages and two unpack
+    groups; wider one group beside fewer than four stages."""
+    if L["max_nb_pass"] <= 16:
+        assert (L["ctas_per_sm"], L["unpack_groups"], L["stages"]) == (2, 1, 2), L
+    elif L["max_nb_pass"] <= 64:
+        assert L["ctas_per_sm"] == 1 and L["unpack_groups"] == 2 and L["stages"] >= 4, L
+    else:
+        assert L["ctas_per_sm"] == 1 and L["unpack_groups"] == 1 and L["stages"] < 4, L
+
+
 def test_batch_uneven_shapes(bflib, cuda, oracle):
     rng = np.random.default_rng(2)
     shapes = []
@@ -69,13 +81,32 @@ def test_batch_replay_sees_new_inputs(bflib, cuda, oracle):
 
 def test_batch_narrow_passes_two_groups(bflib, cuda, oracle):
     """Only passes of at most 64 beams (b = 16, 40, 64, and 128 as two passes of
-    64): one grouped launch with four or more unpacked stages and two unpack
-    groups; every problem equals the oracle."""
+    64): the 40- and 64-beam passes run four or more unpacked stages and two
+    unpack groups, the 8- and 16-beam ones the same or, in a launch of their
+    own, two CTAs per SM; every problem equals the oracle."""
     shapes = [(512, 1, 512, 16), (208, 2, 512, 40), (1024, 1, 512, 64), (256, 2, 512, 128), (64, 1, 512, 8)]
     probs = [_problem(bflib, cuda, T, F, D, B, 300 + i) for i, (T, F, D, B) in enumerate(shapes)]
     batch = bflib.Batch([(W, d.ntimes, Ed, Jd) for d, _, W, Ed, Jd in probs])
+    launches = batch.info()["launches"]
+    assert 1 <= len(launches) <= 2 and launches[0]["max_nb_pass"] == 64
+    for L in launches:
+        _check_layout(L)
+    batch.run()
+    bflib.stream_status()
+    for d, (E, A, G), W, Ed, Jd in probs:
+        np.testing.assert_array_equal(Jd.cpu().numpy(), _oracle(oracle, d, E, A, G), err_msg=str(d))
+    batch.close()
+
+
+def test_batch_narrowest_passes_two_ctas_per_sm(bflib, cuda, oracle):
+    """Only passes of at most 16 beams (b = 8, 12, 16, ragged t): one launch of
+    two CTAs per SM; every problem equals the oracle."""
+    shapes = [(4096, 2, 512, 16), (208, 1, 512, 8), (1296, 3, 512, 12), (64, 1, 512, 16), (2048, 1, 512, 16)]
+    probs = [_problem(bflib, cuda, T, F, D, B, 400 + i) for i, (T, F, D, B) in enumerate(shapes)]
+    batch = bflib.Batch([(W, d.ntimes, Ed, Jd) for d, _, W, Ed, Jd in probs])
     (L,) = batch.info()["launches"]
-    assert L["stages"] >= 4 and L["unpack_groups"] == 2 and L["max_nb_pass"] == 64
+    assert L["max_nb_pass"] == 16 and L["problems"] == len(shapes)
+    _check_layout(L)
     batch.run()
     bflib.stream_status()
     for d, (E, A, G), W, Ed, Jd in probs:
@@ -113,11 +144,10 @@ def test_batched_workload_all_problems(bflib, cuda, oracle):
     batch = bflib.Batch([(W, d.ntimes, E, J) for d, W, E, J in probs])
     info = batch.info()
     launches = info["launches"]
-    assert 1 <= len(launches) <= 2 and sum(L["problems"] for L in launches) == len(probs)
+    assert 1 <= len(launches) <= 3 and sum(L["problems"] for L in launches) == len(probs)
     assert sum(L["tiles"] for L in launches) == info["ntiles"]
-    for L in launches:  # four or more unpacked stages run two unpack groups
-        assert L["unpack_groups"] == (2 if L["stages"] >= 4 else 1)
-        assert (L["stages"] >= 4) == (L["max_nb_pass"] <= 64)
+    for L in launches:
+        _check_layout(L)
     batch.run()
     bflib.stream_status()
     assert bench.batched_oracle_check(probs) == len(probs)

@@ -319,6 +319,33 @@ def test_full_size_chunk_matches_reference(bflib, cuda, golden):
     assert cuda.equal(Jt, Js)
 
 
+@pytest.mark.parametrize("B", [16, 8, 12])
+def test_narrowest_passes_large_chunk(bflib, cuda, B):
+    """Passes of at most 16 beams run two CTAs per SM (t=32768 f=8 d=512, seed
+    5: 4096 tiles, ~13 per CTA): the tensor and SIMT kernels agree on every
+    byte, plain and through resident weights."""
+    d = bflib.Dims(32768, 8, 512, 2, B)
+    E, A, G = bflib.seeded_host_inputs(d, 5)
+    Ed, Ad, Gd = _dev(cuda, E), _dev(cuda, A), _dev(cuda, G)
+    Jt = cuda.full((d.jsize,), 0x5A, dtype=cuda.uint8, device="cuda")
+    Js = cuda.full((d.jsize,), 0xA5, dtype=cuda.uint8, device="cuda")
+    bflib.set_kernel("tensor")
+    bflib.form_beams_ex(d, Jt, Ed, Ad, Gd)
+    bflib.set_kernel("simt")
+    bflib.form_beams_ex(d, Js, Ed, Ad, Gd)
+    bflib.set_kernel("auto")
+    bflib.stream_status()
+    assert cuda.equal(Jt, Js)
+    W = bflib.ResidentWeights(8, B, 512, Ad, Gd)
+    try:
+        Jr = cuda.full((d.jsize,), 0x33, dtype=cuda.uint8, device="cuda")
+        W.form_beams(Jr, Ed, 32768)
+        bflib.stream_status()
+        assert cuda.equal(Jr, Js)
+    finally:
+        W.close()
+
+
 def test_wide_array_matches_reference(bflib, cuda, golden):
     """Wide array (t=16384 f=16 d=1024 b=512, seed 4; six beam passes): adler32
     of all of J equals the reference cpu.cxx's, on both kernels."""
@@ -377,11 +404,11 @@ def test_wide_gains_resident_and_plain(bflib, cuda, oracle):
         W.close()
 
 
-@pytest.mark.parametrize("B", [96, 32])
+@pytest.mark.parametrize("B", [96, 32, 16])
 def test_device_wait_timeout_reports_and_recovers(bflib, cuda, oracle, B):
     """A launch whose copies are never issued: its bounded waits expire, the
     call reports ERR_DEVICE_TIMEOUT, and the next launch is correct (b=96: one
-    unpack group; b=32: two groups and the W forwarder)."""
+    unpack group; b=32: two groups and the W forwarder; b=16: two CTAs per SM)."""
     d = bflib.Dims(128, 2, 512, 2, B)
     E, A, G = bflib.seeded_host_inputs(d, 9)
     bflib.set_test_stall(True)
