@@ -1017,7 +1017,7 @@ static cudaError_t plan_launch(TcParams &p, int max_nb_pass, const TcRingPlan &p
   // W slots are reused straight after the tensor core's release (this needs
   // SW <= 2 S, true for every plan here).  Otherwise one group, which hands W
   // slots back S stages late, so at least S slots keep it moving.
-  const int groups = stages >= 4 ? 2 : 1;
+  const int groups = stages >= 4 && !half ? 2 : 1;  // the half-SM layout has one group
   const int st = groups == 2 ? stages : std::min(stages, wslots);
   if (groups == 2 && wslots > 2 * st) return cudaErrorInvalidValue;
   p.max_nb_pass = max_nb_pass;
