@@ -12,7 +12,8 @@ second (one A[f,b,d] * E[t,f,d,p] complex multiply-add; t*f*p*b*d per pass).
 129 MB L2, so no flush is needed); `e2e` times the same pass through the C-ABI
 host-pointer call, copies in and out included.  `--impl reference` times the
 reference's CPU algorithm (the oracle restatement of cpu.cxx) on the host
-cores.  Under torchrun every rank runs its own chunk (frequencies are
+cores; `--impl reference --reference-kernel` times the reference's own exact
+GPU kernel (cuda.cu, wmma s4) compiled unmodified for sm_103a.  Under torchrun every rank runs its own chunk (frequencies are
 independent; no collective), so scaling is weak.
 """
 from __future__ import annotations
@@ -44,6 +45,9 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--reference-kernel", action="store_true",
+                    help="with --impl reference: time the reference's own GPU kernel (cuda.cu, built for sm_103a by "
+                    "oracle/build_ref.sh) instead of its CPU path")
     ap.add_argument("--cpu-seconds", type=float, default=10.0,
                     help="target length of the CPU-baseline sample (the whole chunk when it fits)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -328,6 +332,80 @@ def run_reference(args):
         "adler32_J": f"0x{whole:08x}",
         "parity": {"reference_cpu_cxx_adler32": None if ref is None else f"0x{ref:08x}",
                    "equal": None if ref is None else whole == ref},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_reference_kernel(args):
+    """The reference's own exact GPU kernel (cuda.cu:35-253: wmma s4 MMAs, one
+    block per frequency, launched as cuda.cu:290-296), compiled unmodified for
+    sm_103a by oracle/build_ref.sh, on the same seeded chunk with its inputs
+    resident on the device: CUDA events around K launches after W warm-up
+    launches.  J's adler32 is compared with the reference cpu.cxx's.  Nothing
+    of the GPU library is loaded."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import zlib
+
+    import torch
+
+    from oracle import oracle as O
+    from oracle import ref_gpu
+
+    w = WORKLOAD
+    shape = (w["ntimes"], w["nfrequencies"], w["ndishes"], w["npolarizations"], w["nbeams"])
+    if not ref_gpu.available(*shape):
+        print(json.dumps({"impl": "reference", "unavailable": "the reference GPU kernel is not built for "
+                          f"{shape} (oracle/build_ref.sh builds it where the reference sources are)"}), flush=True)
+        return
+    torch.cuda.set_device(0)
+    od = O.Dims(*shape)
+    E, A, G = O.seeded_inputs(od, w["seed"])
+    Ed, Ad, Gd = (torch.from_numpy(x).cuda() for x in (E, A, G))
+    del E
+    Jd = torch.empty(od.jsize, dtype=torch.uint8, device="cuda")
+    k = ref_gpu.ReferenceKernel(*shape)
+    stream = torch.cuda.current_stream()
+
+    def launch():
+        k.launch(Jd.data_ptr(), Ed.data_ptr(), Ad.data_ptr(), Gd.data_ptr(), stream.cuda_stream)
+
+    for _ in range(max(1, args.warmup)):
+        launch()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        launch()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    adl = zlib.adler32(Jd.cpu().numpy().tobytes())
+    ref = golden_full_adler32()
+    k.close()
+    hbm, kind = load_peaks()
+    alg_bytes = od.esize + od.asize + 4 * od.gsize + od.jsize
+    achieved = alg_bytes / (ms * 1e-3) / 1e9
+    line = {
+        "impl": "reference",
+        "kernel": "cuda.cu form_beams (wmma s4, exact), compiled unmodified for sm_103a",
+        "metric": METRIC,
+        "value": od.cmacs / (ms * 1e-3),
+        "unit": UNIT,
+        "n_gpus": 1,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms, 4),
+        "higher_is_better": True,
+        "dtype": "int4 complex in, int32 sums (wmma s4)",
+        "data": "synthetic (seeded uniform 4-bit complex; G from the reference setup() formula)",
+        "config": {"workload": WORKLOAD_NAME, **WORKLOAD, "launch": "grid f blocks x (4, 8, 12) threads"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                     "frac": round(achieved / hbm, 4), "peak_kind": kind},
+        "adler32_J": f"0x{adl:08x}",
+        "parity": {"reference_cpu_cxx_adler32": None if ref is None else f"0x{ref:08x}",
+                   "equal": None if ref is None else adl == ref},
     }
     print(json.dumps(line), flush=True)
 
@@ -1165,6 +1243,8 @@ def main():
         WORKLOAD_NAME = WORKLOAD_NAME.replace("b=96", f"b={args.beams}")
     if args.profile_kernel:
         profile_kernel(args)
+    elif args.impl == "reference" and args.reference_kernel:
+        run_reference_kernel(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -15,6 +15,11 @@
 #   recipe was written against (/root/reference).
 #   builds   oracle/_ref/<T>_<F>_<D>_<P>_<B>/cpu     (stock program, prints checksum)
 #            oracle/_ref/<T>_<F>_<D>_<P>_<B>/ref_io  (reads E/A/G files, writes J)
+#   and, where nvcc is present, for the shapes the reference's GPU kernel
+#   handles (see GPU_SHAPES), its exact kernel (cuda.cu:35-253) as device code
+#   for sm_103a: oracle/_ref/<shape>/cuda.cubin and the kernel's entry name in
+#   oracle/_ref/<shape>/cuda.entry (from ptxas's own report).  The cubin is not
+#   x86 code, so it also runs on the Arm GPU machine, where the sources are absent.
 set -euo pipefail
 REF=${1:-${BF_REFERENCE_DIR:-/root/reference}}
 HERE=$(cd "$(dirname "$0")" && pwd)
@@ -79,6 +84,30 @@ build_one() {
   g++ $CXXFLAGS -o "$dir/ref_io" "$dir/ref_io_main.o" "$dir/cpu_lib.o" "$dir/arraysizes.o" "$dir/adler32.o"
 }
 
+# The GPU kernel's launch (cuda.cu:290-296: one block per frequency, 4 x 8 x 12
+# threads) covers nbeams only when nbeams / 8 is a multiple of 12 (the assert
+# at cuda.cu:79, compiled out by -DNDEBUG; other beam counts would index past
+# A and J), so only b = 96 shapes are built: the plain-beamform workload, the
+# full single-GPU chunk and a setup()-pattern golden shape.
+GPU_SHAPES=${BF_REF_GPU_SHAPES:-"
+2048 16 512 2 96
+32768 84 512 2 96
+32768 16 512 2 96
+"}
+NVCC=${CUDA_HOME:-/usr/local/cuda}/bin/nvcc
+CUFLAGS="-std=c++17 -Drestrict=__restrict__ --expt-relaxed-constexpr -O3 -DNDEBUG -gencode arch=compute_103a,code=sm_103a"
+
+build_gpu() {
+  local T=$1 F=$2 D=$3 P=$4 B=$5
+  local dir="$OUT/${T}_${F}_${D}_${P}_${B}"
+  if [ -f "$dir/cuda.cubin" ] && [ -f "$dir/cuda.entry" ]; then return 0; fi
+  [ -f "$dir/arraysizes.hxx" ] || return 1
+  "$NVCC" $CUFLAGS -cubin -Xptxas -v -include "$dir/arraysizes.hxx" -I"$REF" "$REF/cuda.cu" \
+    -o "$dir/cuda.cubin" 2> "$dir/cuda_ptxas.txt"
+  sed -nE "s/.*Compiling entry function '([^']+)'.*/\1/p" "$dir/cuda_ptxas.txt" | head -1 > "$dir/cuda.entry"
+  [ -s "$dir/cuda.entry" ]
+}
+
 pids=()
 while read -r T F D P B; do
   [ -z "${T:-}" ] && continue
@@ -87,4 +116,13 @@ while read -r T F D P B; do
 done <<< "$SHAPES"
 rc=0
 for p in "${pids[@]}"; do wait "$p" || rc=1; done
+if [ -x "$NVCC" ]; then
+  pids=()
+  while read -r T F D P B; do
+    [ -z "${T:-}" ] && continue
+    build_gpu "$T" "$F" "$D" "$P" "$B" &
+    pids+=($!)
+  done <<< "$GPU_SHAPES"
+  for p in "${pids[@]}"; do wait "$p" || rc=1; done
+fi
 exit $rc

@@ -208,3 +208,14 @@ def test_A_to_A2_layout(oracle, D):
                     got = signed4(byte >> 4) if i % 2 else signed4(byte & 15)
                     assert got == want
     assert perm == set(range(D))  # a permutation of the dishes
+
+
+def test_reference_gpu_kernel_covers_only_its_launch():
+    """The reference GPU kernel's launch (4 x 8 x 12 threads per frequency,
+    cuda.cu:290-296) covers nbeams only when nbeams / 8 is a multiple of 12;
+    the loader refuses every other shape whether or not a cubin exists."""
+    from oracle import ref_gpu
+
+    for shape in [(2048, 16, 512, 2, 128), (2048, 16, 512, 2, 64), (2048, 16, 512, 2, 100), (2048, 16, 500, 2, 96),
+                  (2044, 16, 512, 2, 96), (2048, 16, 512, 1, 96)]:
+        assert not ref_gpu.available(*shape), shape
