@@ -86,7 +86,7 @@ build_one() {
 
 # The GPU kernel's launch (cuda.cu:290-296: one block per frequency, 4 x 8 x 12
 # threads) covers nbeams only when nbeams / 8 is a multiple of 12 (the assert
-# at cuda.cu:79, compiled out by -DNDEBUG; other beam counts would index past
+# at cuda.cu:76, compiled out by -DNDEBUG; other beam counts would index past
 # A and J), so only b = 96 shapes are built: the plain-beamform workload, the
 # full single-GPU chunk and a setup()-pattern golden shape.
 GPU_SHAPES=${BF_REF_GPU_SHAPES:-"

@@ -7,7 +7,7 @@ it.  This module loads that cubin through the CUDA driver API into the calling
 thread's current context (the one PyTorch made current) and launches it the
 way the reference's main does (cuda.cu:290-296): one block per frequency,
 4 x 8 x 12 threads, no dynamic shared memory.  The launch covers every beam
-only when nbeams / 8 is a multiple of 12 (cuda.cu:79), which `available`
+only when nbeams / 8 is a multiple of 12 (cuda.cu:76), which `available`
 checks before anything runs.
 
 Only the tests and the benchmark's reference arm use it, as a second
@@ -20,7 +20,7 @@ import os
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _REF_DIR = os.path.join(_HERE, "_ref")
-_BLOCK = (4, 8, 12)  # cuda.cu:294
+_BLOCK = (4, 8, 12)  # cuda.cu:295
 
 
 def shape_dir(ntimes: int, nfrequencies: int, ndishes: int, npolarizations: int, nbeams: int) -> str:
@@ -29,7 +29,7 @@ def shape_dir(ntimes: int, nfrequencies: int, ndishes: int, npolarizations: int,
 
 def available(ntimes: int, nfrequencies: int, ndishes: int, npolarizations: int, nbeams: int) -> bool:
     """True when the cubin for this shape was built and the reference's launch
-    covers the shape exactly (cuda.cu:66-79)."""
+    covers the shape exactly (cuda.cu:63-76)."""
     if nbeams % 8 or (nbeams // 8) % _BLOCK[2] or ndishes % 32 or ntimes % 8 or npolarizations != 2:
         return False
     d = shape_dir(ntimes, nfrequencies, ndishes, npolarizations, nbeams)
