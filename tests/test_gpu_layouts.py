@@ -9,7 +9,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-SHAPES = [(256, 2, 512, 96), (128, 3, 256, 40), (192, 1, 512, 200)]
+SHAPES = [(256, 2, 512, 96), (128, 3, 256, 40), (192, 1, 512, 200), (320, 2, 512, 16)]
 
 
 def _inputs(bflib, T, F, D, B, seed):
