@@ -19,7 +19,7 @@
 #   handles (see GPU_SHAPES), its exact kernel (cuda.cu:35-253) as device code
 #   for sm_103a: oracle/_ref/<shape>/cuda.cubin and the kernel's entry name in
 #   oracle/_ref/<shape>/cuda.entry (from ptxas's own report).  The cubin is not
-#   x86 code, so it also runs on the Arm GPU machine, where the sources are absent.
+#   x86 code, so it also runs on an Arm host, where the reference sources are absent.
 set -euo pipefail
 REF=${1:-${BF_REFERENCE_DIR:-/root/reference}}
 HERE=$(cd "$(dirname "$0")" && pwd)
