@@ -436,8 +436,9 @@ __global__ void __launch_bounds__(Roles<kEpiW, kGroups>::kThreads, kHalf ? 2 : 1
           const int s = static_cast<int>(wr.idx);
           if constexpr (RL::kForwarder) {
             // the slot held sequence it - SW: free once the tensor core finished
-            // that stage (its commit on empty).  SW <= 2 S, so that barrier cannot
-            // have moved two phases past the one waited for.
+            // that stage (its commit on empty).  SW <= S, so the stage's next use
+            // (sequence it - SW + S) is not loaded yet and the barrier cannot be a
+            // phase past the one waited for.
             if (it >= static_cast<uint32_t>(SW)) {
               const uint32_t j = it - static_cast<uint32_t>(SW);
               if (!mbar_wait(empty(static_cast<int>(j % static_cast<uint32_t>(S))), (j / static_cast<uint32_t>(S)) & 1u,
@@ -1004,22 +1005,25 @@ static cudaError_t plan_launch(TcParams &p, int max_nb_pass, const TcRingPlan &p
   const int per_half = (acc_cols - 2 * max_nb_pass) / kStageCols;
   const int stages = std::min(kMaxStages, 2 * per_half);
   if (stages < 2) return cudaErrorInvalidValue;
+  // Four or more unpacked stages: two unpack groups and the W forwarder.  Its
+  // W producer reuses the slot of sequence it - SW once the tensor core's
+  // commit of that sequence's stage arrives on `empty`, a parity wait that
+  // must not find the stage's next use (sequence it - SW + S) committed too,
+  // so SW <= S.  Otherwise one group, which hands W slots back S stages late,
+  // so at least S slots keep it moving.
+  const int groups = stages >= 4 && !half ? 2 : 1;  // the half-SM layout has one group
   // shared memory: W slots first (their loads gate the MMA), then raw E slots
   const int want_w = plan.wslots > 0 ? plan.wslots : g_plan_wslots;
   const int want_r = plan.raw > 0 ? plan.raw : g_plan_raw;
   int wslots = want_w > 0 ? want_w : kMaxWSlots;
+  if (groups == 2) wslots = std::min(wslots, stages);
   int raw = want_r > 0 ? want_r : kMinRaw;
   while (wslots > 2 && smem_plan(stages, wslots, raw, max_nb_pass).total + 1024 > smem_limit) --wslots;
   while (raw < kMaxRaw && smem_plan(stages, wslots, raw + 1, max_nb_pass).total + 1024 <= smem_limit && want_r <= 0)
     ++raw;
   while (raw > 2 && smem_plan(stages, wslots, raw, max_nb_pass).total + 1024 > smem_limit) --raw;
-  // Four or more unpacked stages: two unpack groups and the W forwarder, whose
-  // W slots are reused straight after the tensor core's release (this needs
-  // SW <= 2 S, true for every plan here).  Otherwise one group, which hands W
-  // slots back S stages late, so at least S slots keep it moving.
-  const int groups = stages >= 4 && !half ? 2 : 1;  // the half-SM layout has one group
   const int st = groups == 2 ? stages : std::min(stages, wslots);
-  if (groups == 2 && wslots > 2 * st) return cudaErrorInvalidValue;
+  if (groups == 2 && wslots > st) return cudaErrorInvalidValue;
   p.max_nb_pass = max_nb_pass;
   p.stages = st;
   p.wslots = wslots;
