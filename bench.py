@@ -607,8 +607,11 @@ def run_ours(args):
         n_e = max(3, min(args.steps, 20))
         barrier()
         t0 = time.perf_counter()
+        passes = []
         for _ in range(n_e):
+            tp = time.perf_counter()
             bf.form_beams_ex(d, Jn, En, An, Gn)
+            passes.append(time.perf_counter() - tp)
         barrier()
         e_s = (time.perf_counter() - t0) / n_e
         import zlib
@@ -618,6 +621,8 @@ def run_ours(args):
             "value": d.cmacs * world / e_s,
             "unit": UNIT,
             "ms_per_step": round(1e3 * e_s, 3),
+            "pass_ms_median": round(1e3 * statistics.median(passes), 3),
+            "pass_ms_min": round(1e3 * min(passes), 3),
             "h2d_bytes_per_step": d.esize + d.asize + 4 * d.gsize,
             "d2h_bytes_per_step": d.jsize,
             "api": "bf_form_beams_ex(ptr_kind=BF_PTR_HOST), pinned host buffers",
