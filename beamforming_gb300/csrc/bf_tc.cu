@@ -472,6 +472,7 @@ __global__ void __launch_bounds__(Roles<kEpiW, kGroups>::kThreads, kHalf ? 2 : 1
       const uint64_t a_const = smem_desc_sw32(smem_u32(sA));
       const uint64_t w_desc0 = smem_desc_sw128(smem_u32(sW));
       uint32_t local = 0;
+      uint32_t nstage = 0, ndig = 0, nacc = 0;  // commits issued on empty, d_empty, accfull
       bool ok = true;
       const TileRange tr = TileRange::of<kGrouped>(p);
       ProblemCursor<kGrouped> pc;
@@ -490,6 +491,7 @@ __global__ void __launch_bounds__(Roles<kEpiW, kGroups>::kThreads, kHalf ? 2 : 1
         // the offset MMA starts the accumulator at -8 sum_k W[n][k] / 512
         mma_f8f6f4(d_tmem, a_const, smem_desc_sw32(smem_u32(sD + ds * sp.dbytes)), idesc, 0u);
         mma_commit(d_empty(ds));
+        ++ndig;
         dr.advance();
         for (int ks = 0; ks < p.nk; ++ks, ar.advance(), wr.advance()) {
           const int s = static_cast<int>(ar.idx);
@@ -504,10 +506,24 @@ __global__ void __launch_bounds__(Roles<kEpiW, kGroups>::kThreads, kHalf ? 2 : 1
           const uint64_t b_desc = w_desc0 + static_cast<uint64_t>((sw * sp.wbytes) >> 4);
           mma_ts_stage8(d_tmem, a_tmem, b_desc, b_desc + static_cast<uint64_t>(wbox >> 4), idesc);
           mma_commit(empty(s));  // also frees the W slot: the unpack passes it on
+          ++nstage;
         }
         if (!ok) break;
         mma_commit(accfull(ab));
+        ++nacc;
       }
+      // A commit's arrival is an asynchronous write into this CTA's shared
+      // memory, and nothing waits for the last ones on each stage and digit
+      // slot: wait for the last phase committed on every barrier (bounded)
+      // before the CTA can exit.  On the error path this also lets the MMAs
+      // already issued finish before the tensor memory is freed.
+      const uint32_t uS = static_cast<uint32_t>(S), uD = static_cast<uint32_t>(kDigSlots);
+      for (uint32_t k = nstage > uS ? nstage - uS : 0; k < nstage; ++k)
+        mbar_wait_drain(empty(static_cast<int>(k % uS)), (k / uS) & 1u);
+      for (uint32_t k = ndig > uD ? ndig - uD : 0; k < ndig; ++k)
+        mbar_wait_drain(d_empty(static_cast<int>(k % uD)), (k / uD) & 1u);
+      for (uint32_t k = nacc > 2u ? nacc - 2u : 0u; k < nacc; ++k)
+        mbar_wait_drain(accfull(static_cast<int>(k & 1u)), (k >> 1) & 1u);
     }
   } else if (RL::kForwarder && warp == RL::kFwdWarp) {
     // ------------------------------------------------------------ W forwarder
