@@ -50,6 +50,33 @@ TC_SHAPES = [
 ]
 
 
+def _random_tc_shapes(n=40, seed=20261204):
+    """Seeded shapes across every layout the tensor-core kernel picks: beam
+    counts 1-300 (passes of 8-96 beams: two CTAs per SM, two unpack groups
+    with the W forwarder, one group; ragged beams and several passes), dish
+    counts 8-2048 (partial last K stage), 16-512 times (partial last time
+    tile), 1-3 frequencies; sized so that the oracle finishes each in well
+    under a second."""
+    rng = np.random.default_rng(seed)
+    shapes = []
+    while len(shapes) < n:
+        D = int(rng.integers(1, 257)) * 8
+        B = int(rng.integers(1, 301))
+        T = int(rng.integers(1, 33)) * 16
+        F = int(rng.integers(1, 4))
+        if T * F * 2 * B * D <= 4e7:
+            shapes.append((T, F, D, 2, B))
+    return shapes
+
+
+@pytest.mark.parametrize("shape", _random_tc_shapes())
+def test_random_shapes_tensor_vs_oracle(bflib, cuda, oracle, shape):
+    d = bflib.Dims(*shape)
+    E, A, G = bflib.seeded_host_inputs(d, sum(shape))
+    J = run_gpu(bflib, cuda, d, E, A, G, "tensor")
+    np.testing.assert_array_equal(J, oracle.form_beams(oracle_dims(oracle, d), E, A, G), err_msg=str(shape))
+
+
 @pytest.mark.parametrize("shape", TC_SHAPES)
 @pytest.mark.parametrize("kernel", ["tensor", "simt"])
 def test_seeded_shapes_match_oracle(bflib, cuda, oracle, shape, kernel):
