@@ -60,6 +60,8 @@ def parse_args():
     ap.add_argument("--frequencies", type=int, default=None, help="override f (profiling a smaller case)")
     ap.add_argument("--beams", type=int, default=None,
                     help="override b (profiling: b <= 64 runs the two-unpack-group layout)")
+    ap.add_argument("--dishes", type=int, default=None, help="override d (profiling the wide-array kernel)")
+    ap.add_argument("--times", type=int, default=None, help="override t (profiling)")
     ap.add_argument(
         "--workload",
         choices=["chunk", "batched", "served", "wide"],
@@ -1260,6 +1262,12 @@ def main():
     if args.beams:
         WORKLOAD["nbeams"] = args.beams
         WORKLOAD_NAME = WORKLOAD_NAME.replace("b=96", f"b={args.beams}")
+    if args.dishes:
+        WORKLOAD["ndishes"] = args.dishes
+        WORKLOAD_NAME = WORKLOAD_NAME.replace("d=512", f"d={args.dishes}")
+    if args.times:
+        WORKLOAD["ntimes"] = args.times
+        WORKLOAD_NAME = WORKLOAD_NAME.replace("t=32768", f"t={args.times}")
     if args.profile_kernel:
         profile_kernel(args)
     elif args.impl == "reference" and args.reference_kernel:
