@@ -68,8 +68,10 @@ EXPORTED_SYMBOLS = (
     "bf_server_wait",
     "bf_server_drain",
     "bf_server_stats_get",
+    "bf_server_replay",
     "bf_server_destroy",
     "bf_adler32_device",
+    "bf_adler32_host",
     "bf_fill_random_device",
     "bf_fill_random_host",
     "bf_gains_host",
@@ -185,6 +187,12 @@ def lib() -> ctypes.CDLL:
         L.bf_server_wait.argtypes = [vp, ctypes.c_int64, ctypes.POINTER(ctypes.c_double)]
         L.bf_server_drain.argtypes = [vp]
         L.bf_server_stats_get.argtypes = [vp, ctypes.POINTER(_ServerStats)]
+        dp = ctypes.POINTER(ctypes.c_double)
+        L.bf_server_replay.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int64),
+                                       ctypes.POINTER(vp), ctypes.c_int, ctypes.POINTER(vp), ctypes.c_int,
+                                       ctypes.POINTER(ctypes.c_int64), ctypes.c_int, dp, ctypes.c_int, dp, dp,
+                                       ctypes.POINTER(ctypes.c_uint32), dp, ctypes.POINTER(ctypes.c_int64)]
+        L.bf_adler32_host.argtypes = [u8p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_uint32)]
         L.bf_server_destroy.argtypes = [vp]
         L.bf_adler32_device.argtypes = [u8p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_uint32), vp]
         L.bf_fill_random_device.argtypes = [u8p, ctypes.c_size_t, ctypes.c_uint64, ctypes.c_uint64, vp]
@@ -453,6 +461,46 @@ class Server:
     def drain(self) -> None:
         _check(lib().bf_server_drain(self._h), "bf_server_drain")
 
+    def replay(self, channels, ntimes, E_list, J_slots, j_bytes, arrivals, check_threads: int = 4) -> dict:
+        """Native load generator (bf_server_replay): chunk i (channel
+        ``channels[i]``, ``ntimes[i]`` samples, input ``E_list[i]``, pinned
+        host numpy arrays or CUDA tensors) is submitted ``arrivals[i]`` seconds
+        after the call into J slot ``J_slots[i % len(J_slots)]`` (host numpy
+        views, ``j_bytes[i]`` bytes used); returns per-chunk latency and
+        lateness (seconds) and the adler32 of each landed J, the wall time to
+        the last completion and the number of slot waits."""
+        n = len(arrivals)
+        w = self.weights
+        ch = (ctypes.c_int * n)(*[int(c) for c in channels])
+        nt = (ctypes.c_int64 * n)(*[int(t) for t in ntimes])
+        jb = (ctypes.c_int64 * n)(*[int(b) for b in j_bytes])
+        arr = (ctypes.c_double * n)(*[float(a) for a in arrivals])
+        eptr, ekind = [], None
+        for e, t in zip(E_list, ntimes):
+            p, k = _ptr(e, np.uint8, int(t) * w.ndishes * 2)
+            eptr.append(int(p))
+            ekind = k if ekind is None else ekind
+            if k != ekind:
+                raise ValueError("E inputs must all be host arrays or all CUDA tensors")
+        jptr, jkind = [], None
+        for js in J_slots:
+            p, k = _ptr(js, np.uint8, js.nbytes if hasattr(js, "nbytes") else js.numel(), writable=True)
+            jptr.append(int(p))
+            jkind = k if jkind is None else jkind
+        E_arr = (ctypes.c_void_p * n)(*eptr)
+        J_arr = (ctypes.c_void_p * len(jptr))(*jptr)
+        lat = np.zeros(n)
+        late = np.zeros(n)
+        adl = np.zeros(n, dtype=np.uint32)
+        wall = ctypes.c_double()
+        stalls = ctypes.c_int64()
+        dp = ctypes.POINTER(ctypes.c_double)
+        _check(lib().bf_server_replay(
+            self._h, n, ch, nt, E_arr, ekind, J_arr, len(jptr), jb, jkind, arr, check_threads,
+            lat.ctypes.data_as(dp), late.ctypes.data_as(dp), adl.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
+            ctypes.byref(wall), ctypes.byref(stalls)), "bf_server_replay")
+        return {"latency_s": lat, "late_s": late, "adler32": adl, "wall_s": wall.value, "slot_stalls": stalls.value}
+
     def stats(self) -> dict:
         st = _ServerStats()
         _check(lib().bf_server_stats_get(self._h, ctypes.byref(st)), "bf_server_stats_get")
@@ -537,6 +585,14 @@ def tensor_peak_tflops(stream=None) -> float:
     out = ctypes.c_double()
     _check(lib().bf_tensor_peak(ctypes.byref(out), _stream_handle(stream)), "bf_tensor_peak")
     return out.value
+
+
+def adler32_host(data) -> int:
+    """adler32 (adler32.c:7-20) of a host uint8 array, computed by the library."""
+    a = np.ascontiguousarray(data, dtype=np.uint8)
+    out = ctypes.c_uint32()
+    _check(lib().bf_adler32_host(a.ctypes.data, a.nbytes, ctypes.byref(out)), "bf_adler32_host")
+    return int(out.value)
 
 
 def adler32_device(data, nbytes: int | None = None, stream=None) -> int:

@@ -152,4 +152,31 @@ cudaError_t launch_fill_random(uint8_t *dst, size_t n, uint64_t seed, uint64_t s
   return cudaGetLastError();
 }
 
+uint32_t adler32_host(const uint8_t *p, size_t n) {
+  uint32_t a = 1, b = 0;
+  while (n > 0) {
+    // 5552 bytes is the longest run whose sums cannot overflow 32 bits
+    // before the reduction (255 n (n + 1) / 2 + (n + 1) (65521 - 1) < 2^32)
+    size_t k = n < 5552 ? n : 5552;
+    n -= k;
+    for (; k >= 8; k -= 8, p += 8) {
+      a += p[0]; b += a; a += p[1]; b += a; a += p[2]; b += a; a += p[3]; b += a;
+      a += p[4]; b += a; a += p[5]; b += a; a += p[6]; b += a; a += p[7]; b += a;
+    }
+    for (; k > 0; --k) {
+      a += *p++;
+      b += a;
+    }
+    a %= kAdlerMod;
+    b %= kAdlerMod;
+  }
+  return (b << 16) | a;
+}
+
 }  // namespace bf
+
+extern "C" int bf_adler32_host(const uint8_t *data, size_t len, uint32_t *out) {
+  if (!out || (len && !data)) return BF_ERR_INVALID_ARGUMENT;
+  *out = bf::adler32_host(data, len);
+  return BF_OK;
+}

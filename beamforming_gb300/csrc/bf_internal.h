@@ -194,6 +194,8 @@ int adler_nchunks(size_t len);
 cudaError_t launch_adler_partials(const uint8_t *data, size_t len, uint32_t *partials, cudaStream_t s);
 // Combines the partials into one adler32 value in *out (device).
 cudaError_t launch_adler_combine(const uint32_t *partials, size_t len, uint32_t *out, cudaStream_t s);
+// adler32 of n bytes of host memory (adler32.c:7-20).
+uint32_t adler32_host(const uint8_t *p, size_t n);
 
 // Workload generator.
 cudaError_t launch_fill_random(uint8_t *dst, size_t n, uint64_t seed, uint64_t stream_id, cudaStream_t s);

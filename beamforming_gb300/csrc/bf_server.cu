@@ -576,6 +576,124 @@ int bf_server_drain(bf_server *s) {
   return s->status;
 }
 
+int bf_server_replay(bf_server *s, int n, const int *channel, const int64_t *ntimes, const uint8_t *const *E,
+                     int e_on_device, uint8_t *const *J_slots, int nslots, const int64_t *j_bytes, int j_on_device,
+                     const double *arrival_s, int check_threads, double *latency_s, double *late_s,
+                     uint32_t *adler_out, double *wall_s, int64_t *slot_stalls) {
+  if (!s || n < 0 || check_threads < 0 || !wall_s) return BF_ERR_INVALID_ARGUMENT;
+  if (n > 0 && (!channel || !ntimes || !E || !J_slots || nslots <= 0 || !j_bytes || !arrival_s || !latency_s))
+    return BF_ERR_INVALID_ARGUMENT;
+  if (check_threads > 0 && (j_on_device || !adler_out)) return BF_ERR_INVALID_ARGUMENT;
+  *wall_s = 0.0;
+  if (slot_stalls) *slot_stalls = 0;
+  if (n == 0) return BF_OK;
+
+  std::vector<int64_t> tickets(static_cast<size_t>(n), -1);
+  // slot k may take chunk i once chunk i - nslots, its previous user, is done
+  // (landed, and checked when checking); done_upto[k] is the last such chunk
+  std::vector<int64_t> done_upto(static_cast<size_t>(nslots), -1);
+  std::mutex m;
+  std::condition_variable cv_pub, cv_check, cv_free;
+  int published = 0;        // chunks submitted (their tickets are valid)
+  bool waiter_done = false;
+  std::deque<int> to_check;
+  std::atomic<int> status{BF_OK};
+  const auto t0 = Clock::now();
+  Clock::time_point t_last = t0;
+
+  auto release_slot = [&](int i) {
+    std::lock_guard<std::mutex> lk(m);
+    int64_t &d = done_upto[static_cast<size_t>(i % nslots)];
+    d = std::max<int64_t>(d, i);
+    cv_free.notify_all();
+  };
+  std::thread waiter([&] {
+    for (int i = 0; i < n; ++i) {
+      {
+        std::unique_lock<std::mutex> lk(m);
+        cv_pub.wait(lk, [&] { return published > i || status.load() != BF_OK; });
+        if (published <= i) break;  // the submitter stopped
+      }
+      double lat = 0.0;
+      const int st = bf_server_wait(s, tickets[static_cast<size_t>(i)], &lat);
+      if (st != BF_OK) {
+        status.store(st);
+        break;
+      }
+      latency_s[i] = lat;
+      t_last = Clock::now();
+      if (check_threads > 0) {
+        std::lock_guard<std::mutex> lk(m);
+        to_check.push_back(i);
+        cv_check.notify_one();
+      } else {
+        release_slot(i);
+      }
+    }
+    std::lock_guard<std::mutex> lk(m);
+    waiter_done = true;
+    cv_check.notify_all();
+    cv_free.notify_all();
+  });
+  std::vector<std::thread> checkers;
+  for (int c = 0; c < check_threads; ++c)
+    checkers.emplace_back([&] {
+      for (;;) {
+        int i;
+        {
+          std::unique_lock<std::mutex> lk(m);
+          cv_check.wait(lk, [&] { return !to_check.empty() || waiter_done; });
+          if (to_check.empty()) return;
+          i = to_check.front();
+          to_check.pop_front();
+        }
+        adler_out[i] = adler32_host(J_slots[i % nslots], static_cast<size_t>(j_bytes[i]));
+        release_slot(i);
+      }
+    });
+
+  int64_t stalls = 0;
+  for (int i = 0; i < n && status.load() == BF_OK; ++i) {
+    const int k = i % nslots;
+    {
+      std::unique_lock<std::mutex> lk(m);
+      if (done_upto[static_cast<size_t>(k)] < i - nslots) {
+        ++stalls;
+        cv_free.wait(lk, [&] {
+          return done_upto[static_cast<size_t>(k)] >= i - nslots || status.load() != BF_OK || waiter_done;
+        });
+        if (done_upto[static_cast<size_t>(k)] < i - nslots) break;
+      }
+    }
+    // sleep to just before the arrival time, then spin to it
+    const auto due = t0 + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(arrival_s[i]));
+    const auto ahead = due - Clock::now();
+    if (ahead > std::chrono::microseconds(300)) std::this_thread::sleep_for(ahead - std::chrono::microseconds(200));
+    while (Clock::now() < due) {
+    }
+    int64_t tk = -1;
+    const int st = bf_server_submit(s, channel[i], 1, ntimes[i], E[i], e_on_device, J_slots[k], j_on_device, &tk);
+    if (late_s) late_s[i] = std::chrono::duration<double>(Clock::now() - due).count();
+    if (st != BF_OK) {
+      status.store(st);
+      break;
+    }
+    std::lock_guard<std::mutex> lk(m);
+    tickets[static_cast<size_t>(i)] = tk;
+    published = i + 1;
+    cv_pub.notify_one();
+  }
+  {
+    std::lock_guard<std::mutex> lk(m);
+    cv_pub.notify_all();  // a failed submission ends the waiter too
+  }
+  waiter.join();
+  for (auto &t : checkers) t.join();
+  *wall_s = std::chrono::duration<double>(t_last - t0).count();
+  if (slot_stalls) *slot_stalls = stalls;
+  return status.load();
+}
+
 int bf_server_stats_get(bf_server *s, bf_server_stats *out) {
   if (!s || !out) return BF_ERR_INVALID_ARGUMENT;
   std::lock_guard<std::mutex> lk(s->mu);

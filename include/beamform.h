@@ -287,6 +287,24 @@ BF_API int bf_server_drain(bf_server *server);
 
 BF_API int bf_server_stats_get(bf_server *server, bf_server_stats *stats);
 
+/* A load generator for measuring a server without an interpreter in the
+ * loop.  Chunk i (one channel channel[i], ntimes[i] samples, input E[i]) is
+ * submitted by the calling thread arrival_s[i] seconds after the call (all 0:
+ * back to back) into J slot i % nslots (J_slots[k], j_bytes[i] bytes used);
+ * a native thread waits for the chunks in order and stores each latency
+ * (submission to completion) in latency_s[i], and check_threads native threads
+ * (0: none) store the adler32 of each landed J in adler_out[i] before its slot
+ * is given to a later chunk (a submission waits for that: *slot_stalls counts
+ * the waits).  late_s[i] (may be NULL) is how late chunk i was submitted.
+ * Returns when every chunk is complete and checked, with the time from the
+ * call to the last completion in *wall_s.  Checking needs J in host memory.
+ * No counterpart in the reference. */
+BF_API int bf_server_replay(bf_server *server, int n, const int *channel, const int64_t *ntimes,
+                            const uint8_t *const *E, int e_on_device, uint8_t *const *J_slots, int nslots,
+                            const int64_t *j_bytes, int j_on_device, const double *arrival_s, int check_threads,
+                            double *latency_s, double *late_s, uint32_t *adler_out, double *wall_s,
+                            int64_t *slot_stalls);
+
 BF_API int bf_server_destroy(bf_server *server);
 
 /* ------------------------------------------------------- no allocation */
@@ -318,6 +336,9 @@ BF_API int bf_form_beams_noalloc(const bf_dims *dims, uint8_t *J, const uint8_t 
 /* adler32 (adler32.c:7-20) of `len` bytes of device memory; the result is
  * written to *out (host).  Synchronous on `stream`. */
 BF_API int bf_adler32_device(const uint8_t *data, size_t len, uint32_t *out, bf_stream_t stream);
+
+/* adler32 of `len` bytes of host memory on the calling thread; needs no device. */
+BF_API int bf_adler32_host(const uint8_t *data, size_t len, uint32_t *out);
 
 /* ------------------------------------------------------- workload generator */
 

@@ -93,6 +93,20 @@ def test_invalid_arguments(bflib):
     assert L.bf_server_wait(None, 0, None) == bflib.ERR_INVALID_ARGUMENT
     assert L.bf_server_drain(None) == bflib.ERR_INVALID_ARGUMENT
     assert L.bf_server_destroy(None) == bflib.OK
+    wall = ctypes.c_double()
+    assert L.bf_server_replay(None, 0, None, None, None, 0, None, 0, None, 0, None, 0, None, None, None,
+                              ctypes.byref(wall), None) == bflib.ERR_INVALID_ARGUMENT
+
+
+@pytest.mark.parametrize("n", [0, 1, 7, 5551, 5552, 5553, 3 * 5552 + 11, (1 << 20) + 7])
+def test_host_adler32_matches_zlib(bflib, n):
+    """bf_adler32_host (no device) equals zlib's adler32 across the 5552-byte
+    reduction blocks, on all-0xFF bytes (the largest sums) and random bytes."""
+    import zlib
+
+    rng = np.random.default_rng(n)
+    for data in (np.full(n, 255, np.uint8), rng.integers(0, 256, n, dtype=np.uint8)):
+        assert bflib.adler32_host(data) == zlib.adler32(data.tobytes())
 
 
 def test_python_argument_checks(bflib):

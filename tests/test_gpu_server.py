@@ -180,3 +180,40 @@ def test_server_small_staging_ring_back_pressure(bflib, oracle, weights):
     assert st["staged"] == len(chunks)
     for (c0, nch, T, E), J in zip(chunks, outs):
         np.testing.assert_array_equal(J, _expected(oracle, A, G, c0, nch, T, E))
+
+
+@pytest.mark.parametrize("max_batch,max_inflight,nslots,rate", [(0, 0, 5, 0.0), (1, 1, 5, 0.0), (0, 0, 64, 4000.0)])
+def test_server_replay_native_load_generator(bflib, cuda, oracle, weights, max_batch, max_inflight, nslots, rate):
+    """bf_server_replay submits on a schedule from native threads, reuses its
+    J slots only after the previous chunk in the slot landed and was
+    checksummed, and returns each landed J's adler32: every one equals the
+    oracle's for its chunk (back to back with 5 slots, so submissions wait
+    for slots; and a Poisson stream)."""
+    import zlib
+
+    import torch
+
+    W, A, G = weights
+    rng = np.random.default_rng(17)
+    contents = []
+    for k in range(6):
+        c0 = int(rng.integers(0, F))
+        T = int(rng.choice([64, 256, 1024]))
+        E = torch.empty(T * D * 2, dtype=torch.uint8, pin_memory=True).numpy()
+        bflib.fill_random_host(E, 500 + k, 0)
+        contents.append((c0, T, E, zlib.adler32(_expected(oracle, A, G, c0, 1, T, E).tobytes())))
+    n = 60
+    picks = rng.integers(len(contents), size=n)
+    arrivals = np.zeros(n) if rate == 0 else np.cumsum(rng.exponential(1.0 / rate, n))
+    maxj = B * 2 * 1024
+    ring = torch.empty(nslots * maxj, dtype=torch.uint8, pin_memory=True).numpy()
+    slots = [ring[k * maxj:(k + 1) * maxj] for k in range(nslots)]
+    srv = bflib.Server(W, max_batch=max_batch, max_inflight=max_inflight)
+    r = srv.replay([contents[p][0] for p in picks], [contents[p][1] for p in picks], [contents[p][2] for p in picks],
+                   slots, [B * 2 * contents[p][1] for p in picks], arrivals, check_threads=3)
+    st = srv.stats()
+    srv.close()
+    assert [int(a) for a in r["adler32"]] == [contents[p][3] for p in picks]
+    assert st["completed"] == n and (r["latency_s"] > 0).all() and r["wall_s"] > 0
+    if nslots < n and rate == 0:
+        assert r["slot_stalls"] > 0
