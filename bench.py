@@ -881,104 +881,53 @@ def served_setup(bf, torch, ncontents):
 
 def serve_stream(bf, torch, W, contents, arrivals, picks, cfg, nslots, check_threads, pinned=None):
     """Submits chunk `picks[i]` at time `arrivals[i]` (seconds from the start;
-    all zero: back to back) to a server with config `cfg`, checks every
-    landed J against its expected adler32, and returns the measurements.
-    `pinned` is a pinned host buffer for the J slots, reused across calls (a
-    fresh pinned allocation per call lets locked host memory grow from one
-    run to the next); None allocates one."""
-    import queue
-    import threading
-    import zlib
-    from concurrent.futures import ThreadPoolExecutor
-
+    all zero: back to back) to a server with config `cfg` through the
+    library's native load generator (bf_server_replay: the submissions, the
+    in-order waits and the adler32 of every landed J run on native threads),
+    compares every checksum with the chunk's expected one, and returns the
+    measurements.  `pinned` is a pinned host buffer for the J slots, reused
+    across calls (a fresh pinned allocation per call lets locked host memory
+    grow from one run to the next); None allocates one."""
     B = SERVED["nbeams"]
     n = len(arrivals)
     jbytes = np.array([B * 2 * contents[k][1] for k in picks], dtype=np.int64)
     if nslots >= n:
-        # one packed J region per chunk, checked after the stream (no slot ever waits)
+        # one packed J region per chunk: no submission ever waits for a slot
         offs = np.concatenate([[0], np.cumsum(jbytes)])
-        nslots = n
+        size = int(offs[-1])
     else:
-        # a ring of equal slots, each checked and freed as its chunk lands
+        # a ring of equal slots, each checked and given to a later chunk as its chunk lands
         maxj = B * 2 * max(T for _, T, _, _ in contents)
         offs = np.arange(nslots + 1, dtype=np.int64) * maxj
-    if pinned is not None and pinned.size >= int(offs[-1]):
+        size = int(offs[-1])
+    if pinned is not None and pinned.size >= size:
         ring = pinned
     else:
-        ring = torch.empty(int(offs[-1]), dtype=torch.uint8, pin_memory=True).numpy()
-    deferred = nslots == n
-    free = [threading.Event() for _ in range(nslots)]
-    for e in free:
-        e.set()
-    lat = np.zeros(n)
-    late = np.zeros(n)
-    bad = []
+        ring = torch.empty(size, dtype=torch.uint8, pin_memory=True).numpy()
+    slots = [ring[offs[k]:offs[k + 1]] for k in range(min(nslots, n))]
     srv = bf.Server(W, **cfg)
-    handoff: queue.Queue = queue.Queue()
-    pool = ThreadPoolExecutor(check_threads)
-    stalls = 0
-
-    def check(i, slot, jb, want):
-        if zlib.adler32(ring[offs[slot]:offs[slot] + jb]) != want:
-            bad.append(i)
-        free[slot].set()
-
-    def collector():
-        for _ in range(n):
-            i, t, slot, jb, want = handoff.get()
-            lat[i] = srv.wait(t)
-            if not deferred:
-                pool.submit(check, i, slot, jb, want)
-
-    # the submitter spins on the clock holding the GIL; hand the GIL to the
-    # collector and checker threads quickly
-    switch = sys.getswitchinterval()
-    sys.setswitchinterval(5e-5)
-    th = threading.Thread(target=collector)
-    th.start()
-    t0 = time.perf_counter()
-    for i in range(n):
-        c, T, Eh, want = contents[picks[i]]
-        slot = i % nslots
-        if not free[slot].is_set():
-            stalls += 1
-            free[slot].wait()
-        free[slot].clear()
-        due = t0 + arrivals[i]
-        now = time.perf_counter()
-        if due - now > 3e-4:
-            time.sleep(due - now - 2e-4)
-        while time.perf_counter() < due:
-            pass
-        jb = int(jbytes[i])
-        tk = srv.submit(c, T, Eh, ring[offs[slot]:offs[slot] + jb])
-        late[i] = time.perf_counter() - due
-        handoff.put((i, tk, slot, jb, want))
-    srv.drain()
-    t1 = time.perf_counter()
-    th.join()
-    if deferred:
-        for i in range(n):
-            pool.submit(check, i, i, int(jbytes[i]), contents[picks[i]][3])
-    pool.shutdown(wait=True)
-    sys.setswitchinterval(switch)
+    r = srv.replay([contents[k][0] for k in picks], [contents[k][1] for k in picks], [contents[k][2] for k in picks],
+                   slots, jbytes, arrivals, check_threads=check_threads)
     st = srv.stats()
     srv.close()
+    want = np.array([contents[k][3] for k in picks], dtype=np.uint32)
+    bad = int((r["adler32"] != want).sum())
+    lat, late, wall = r["latency_s"], r["late_s"], r["wall_s"]
     Ts = np.array([contents[k][1] for k in picks])
     beam_samples = int(B * 2 * Ts.sum())
     cmac = int(B * 2 * SERVED["ndishes"] * Ts.sum())
     pct = lambda a, q: round(float(np.percentile(a, q)) * 1e3, 3)  # noqa: E731
     return {
         "chunks": n,
-        "wall_s": round(t1 - t0, 3),
-        "chunks_per_s": round(n / (t1 - t0), 1),
-        "beam_samples_per_s": beam_samples / (t1 - t0),
-        "cmac_per_s": cmac / (t1 - t0),
+        "wall_s": round(wall, 3),
+        "chunks_per_s": round(n / wall, 1),
+        "beam_samples_per_s": beam_samples / wall,
+        "cmac_per_s": cmac / wall,
         "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99), "p99.9": pct(lat, 99.9), "max": pct(lat, 100),
                        "mean": round(float(lat.mean()) * 1e3, 3)},
         "submit_lateness_ms": {"p50": pct(late, 50), "p99": pct(late, 99)},
-        "slot_stalls": stalls,
-        "mismatches": len(bad),
+        "slot_stalls": int(r["slot_stalls"]),
+        "mismatches": bad,
         "server": {k: st[k] for k in ("batches", "max_batch_seen", "pool_bytes", "pool_peak_bytes")},
         "config": {k: v for k, v in cfg.items()},
     }
@@ -1072,7 +1021,8 @@ def run_served(args):
         "dtype": "int4 complex in, exact integer sums (e4m3 tensor-core operands, f32 accumulate)",
         "data": "synthetic (seeded uniform 4-bit complex; G from the reference setup() formula)",
         "config": {"workload": SERVED_NAME, "rate_hz": rate, "duration_s": duration,
-                   "distinct_chunks": len(contents), "buffers": "E and J in pinned host memory, copies inside"},
+                   "distinct_chunks": len(contents), "buffers": "E and J in pinned host memory, copies inside",
+                   "load_generator": "bf_server_replay (native submitter, waiter and checksum threads)"},
         "served": sv,
         "plain_loop": pl,
         "served_saturation": out["served_saturation"],
