@@ -82,6 +82,9 @@ def parse_args():
     ap.add_argument("--slots", type=int, default=512, help="served: pinned J slots in the ring")
     ap.add_argument("--check-threads", type=int, default=6, help="served: threads checking landed chunks")
     ap.add_argument("--saturation-chunks", type=int, default=4000, help="served: chunks in the back-to-back run")
+    ap.add_argument("--saturation-probe", action="store_true",
+                    help="served: back-to-back runs alone, with the clock sampler, and after 10 s Poisson streams "
+                    "(what slows later repeats); prints one JSON line")
     ap.add_argument("--extra-rates", type=float, nargs="*", default=[8000.0],
                     help="served: further Poisson rates (chunks/s) run for --extra-duration seconds each")
     ap.add_argument("--extra-duration", type=float, default=5.0)
@@ -947,6 +950,46 @@ def repeat_spread(reps):
     return out
 
 
+def run_saturation_probe(bf, torch, W, contents, sat_picks, cfg, args):
+    """Back-to-back runs of the served loop (fresh server each, checked)
+    alone, twice with the nvidia-smi clock sampler running, and after one and
+    two 10 s Poisson streams at the offered rate: separates the GPU and the
+    server from the host's state after sustained streaming."""
+    S = SERVED
+    nsat = len(sat_picks)
+    maxj = S["nbeams"] * 2 * max(T for _, T, _, _ in contents)
+    sat_pin = torch.empty(sum(S["nbeams"] * 2 * contents[k][1] for k in sat_picks), dtype=torch.uint8,
+                          pin_memory=True).numpy()
+    ring_pin = torch.empty(args.slots * maxj, dtype=torch.uint8, pin_memory=True).numpy()
+    rng = np.random.default_rng(S["seed"] + 2000)
+
+    def sat():
+        r = serve_stream(bf, torch, W, contents, np.zeros(nsat), sat_picks, cfg, nsat, args.check_threads, sat_pin)
+        assert r["mismatches"] == 0
+        return r["beam_samples_per_s"]
+
+    def stream(seconds):
+        n = int(S["rate_hz"] * seconds)
+        arr = np.cumsum(rng.exponential(1.0 / S["rate_hz"], n))
+        arr -= arr[0]
+        r = serve_stream(bf, torch, W, contents, arr, rng.integers(len(contents), size=n), cfg, args.slots,
+                         args.check_threads, ring_pin)
+        assert r["mismatches"] == 0
+        return r["latency_ms"]["p99"]
+
+    out = {"alone": [sat(), sat()]}
+    clocks = ClockSampler(gpu_uuid(torch, 0))
+    clocks.start()
+    out["with_clock_sampler"] = [sat(), sat()]
+    out["clocks"] = clocks.stop()
+    out["stream_1_p99_ms"] = stream(10.0)
+    out["after_stream_1"] = [sat(), sat()]
+    out["stream_2_p99_ms"] = stream(10.0)
+    out["after_stream_2"] = [sat(), sat()]
+    print(json.dumps({"workload": "served saturation probe (beam samples/s of 4000 chunks back to back)",
+                      "config": cfg, **out}), flush=True)
+
+
 def run_served(args):
     """The served stream against the plain per-chunk loop (the same server
     thread with one chunk per launch and one launch in flight), at the
@@ -971,6 +1014,9 @@ def run_served(args):
     served_cfg = {"max_batch": args.max_batch, "max_inflight": args.max_inflight, "spin_wait": not args.no_spin,
                   "hbm_budget_bytes": budget}
     plain_cfg = {"max_batch": 1, "max_inflight": 1, "spin_wait": not args.no_spin, "hbm_budget_bytes": budget}
+    if args.saturation_probe:
+        run_saturation_probe(bf, torch, W, contents, sat_picks, served_cfg, args)
+        return
     out = {}
     reps = {k: [] for k in ("served", "plain", "served_saturation", "plain_saturation")}
     # the J slots of every run live in two pinned buffers allocated once: the
