@@ -52,6 +52,8 @@ def parse_args():
                     help="target length of the CPU-baseline sample (the whole chunk when it fits)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-workloads", action="store_true",
+                    help="chunk workload: skip the compact batched / served / wide records appended to the line")
     ap.add_argument(
         "--profile-kernel",
         action="store_true",
@@ -697,9 +699,59 @@ def run_ours(args):
             "clocks": clk,
             "gpu_launches": 2 * args.steps,
         }
+        if world == 1 and not args.no_workloads:
+            line["workloads"] = other_workloads(args)
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def other_workloads(args):
+    """The batched, served and wide workloads in compact form, so that one
+    default run records all of them (one GPU): the batched set with every
+    problem checked against the oracle, a 10 s served stream plus the
+    back-to-back runs for both loops (every chunk checked), and three rounds
+    of wide-array chunks with weight refresh (every chunk checked).  The full
+    records come from `--workload batched|served|wide`."""
+    import copy
+
+    out = {}
+    a = copy.copy(args)
+    a.steps, a.warmup = 20, 3
+    b = run_batched(a, emit=False)
+    out["batched"] = {
+        "workload": b["config"]["workload"], "value": b["value"], "unit": b["unit"], "ms_per_step": b["ms_per_step"],
+        "roofline_frac": b["roofline"]["frac"], "roofline_bound": b["roofline"]["bound"],
+        "speedup_vs_per_problem": b["speedup_vs_per_problem"],
+        "launches": [(L["problems"], L["max_nb_pass"], L["ctas_per_sm"]) for L in b["autotune"]["launches"]],
+        "parity": b["parity"]}
+    a = copy.copy(args)
+    a.duration, a.repeats, a.extra_rates = 10.0, 1, []
+    sv = run_served(a, emit=False)
+
+    def lat(r):
+        return {q: r["latency_ms"][q] for q in ("p50", "p99", "p99.9")}
+
+    out["served"] = {
+        "workload": sv["config"]["workload"].replace("for 30 s", "for 10 s"), "unit": "beam samples/s",
+        "served": {"latency_ms": lat(sv["served"]), "beam_samples_per_s": sv["served"]["beam_samples_per_s"]},
+        "plain": {"latency_ms": lat(sv["plain_loop"]), "beam_samples_per_s": sv["plain_loop"]["beam_samples_per_s"]},
+        "saturation": {"served": sv["served_saturation"]["beam_samples_per_s"],
+                       "plain": sv["plain_saturation"]["beam_samples_per_s"]},
+        "p99_ratio_plain_over_served": sv["p99_ratio_plain_over_served"],
+        "saturation_speedup": sv["saturation_speedup"],
+        "mismatches": sum(sv[k]["mismatches"] for k in ("served", "plain_loop", "served_saturation",
+                                                        "plain_saturation")),
+        "clocks": sv.get("clocks")}
+    a = copy.copy(args)
+    a.rounds = 3
+    w = run_wide(a, emit=False)
+    out["wide"] = {
+        "workload": w["config"]["workload"], "value": w["value"], "unit": w["unit"], "ms_per_chunk": w["ms_per_step"],
+        "kernel_roofline_frac": w["roofline"]["frac"], "roofline_bound": w["roofline"]["bound"],
+        "kernel_ms": w["roofline"].get("kernel_ms"), "weight_updates": w["served"]["weight_updates"],
+        "mismatches": w["mismatches"], "clocks": w.get("clocks")}
+    return out
 
 
 def profile_kernel(args):
@@ -751,7 +803,7 @@ def batched_oracle_check(probs):
     return ok
 
 
-def run_batched(args):
+def run_batched(args, emit=True):
     """One persistent grouped launch (autotuned, CUDA graph) against the same
     problems launched one by one."""
     import torch
@@ -828,8 +880,10 @@ def run_batched(args):
                   "(adler32)",
         "gpu_launches": args.steps,
     }
-    print(json.dumps(line), flush=True)
+    if emit:
+        print(json.dumps(line), flush=True)
     batch.close()
+    return line
 
 
 SERVED = {"channels": 64, "nbeams": 96, "ndishes": 512, "npolarizations": 2, "rate_hz": 2000.0, "duration_s": 30.0,
@@ -990,7 +1044,7 @@ def run_saturation_probe(bf, torch, W, contents, sat_picks, cfg, args):
                       "config": cfg, **out}), flush=True)
 
 
-def run_served(args):
+def run_served(args, emit=True):
     """The served stream against the plain per-chunk loop (the same server
     thread with one chunk per launch and one launch in flight), at the
     stream's Poisson rate, then back to back (saturation)."""
@@ -1087,7 +1141,9 @@ def run_served(args):
         "clocks": clk,
         "gpu_launches": sv["server"]["batches"],
     }
-    print(json.dumps(line), flush=True)
+    if emit:
+        print(json.dumps(line), flush=True)
+    return line
     W.close()
 
 
@@ -1097,7 +1153,7 @@ WIDE_NAME = ("wide array t=16384 f=16 d=1024 p=2 b=512, seed 4; served loop with
              "8 chunks from seed 4+k")
 
 
-def run_wide(args):
+def run_wide(args, emit=True):
     """Wide-array chunks through the server (device-resident E and J), the
     weights refreshed every 8 chunks without a drain; every chunk's adler32
     against a plain launch with the same weights.  The kernel alone is timed
@@ -1237,7 +1293,9 @@ def run_wide(args):
         "clocks": clk,
         "gpu_launches": st["batches"],
     }
-    print(json.dumps(line), flush=True)
+    if emit:
+        print(json.dumps(line), flush=True)
+    return line
 
 
 def main():
