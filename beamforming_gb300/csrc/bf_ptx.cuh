@@ -83,15 +83,31 @@ __device__ __forceinline__ bool mbar_try_wait_sleep(uint32_t bar, uint32_t parit
 // hardware ends a suspended try_wait long before the hint, so the error word
 // and the clock are read only every kPollCheck polls: reading them on every
 // poll took a fifth of the issue slots of the tensor-core kernel.
+//
+// The clock (%globaltimer) is not trusted alone: a wait expires only after
+// kMinTimeoutPolls polls as well (milliseconds of polling; no wait of a working
+// pipeline lasts that long), and a clock that steps back restarts the window.
+// A time difference taken in unsigned arithmetic across a backward step would
+// wrap to ~2^64 and end a healthy wait at once.
 constexpr uint32_t kPollCheck = 16;
+constexpr uint32_t kMinTimeoutPolls = 4096;
+__device__ __forceinline__ bool wait_expired(uint64_t &t0, uint32_t polls) {
+  const uint64_t now = globaltimer_ns();
+  if (now < t0) {  // the clock stepped back: restart the window
+    t0 = now;
+    return false;
+  }
+  return polls >= kMinTimeoutPolls && now - t0 > kWaitTimeoutNs;
+}
+
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int *err, int code) {
   if (mbar_try_wait(bar, parity)) return true;
-  const uint64_t t0 = globaltimer_ns();
+  uint64_t t0 = globaltimer_ns();
   for (uint32_t i = 1;; ++i) {
     if (mbar_try_wait_sleep(bar, parity, 200000u)) return true;
     if (i % kPollCheck == 0) {
       if (*reinterpret_cast<volatile int *>(err) != 0) return false;
-      if (globaltimer_ns() - t0 > kWaitTimeoutNs) {
+      if (wait_expired(t0, i)) {
         atomicCAS(err, 0, code);
         return false;
       }
@@ -104,10 +120,10 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int *er
 // CTA exits (at most kWaitTimeoutNs per barrier).
 __device__ __forceinline__ bool mbar_wait_drain(uint32_t bar, uint32_t parity) {
   if (mbar_try_wait(bar, parity)) return true;
-  const uint64_t t0 = globaltimer_ns();
+  uint64_t t0 = globaltimer_ns();
   for (uint32_t i = 1;; ++i) {
     if (mbar_try_wait_sleep(bar, parity, 200000u)) return true;
-    if (i % kPollCheck == 0 && globaltimer_ns() - t0 > kWaitTimeoutNs) return false;
+    if (i % kPollCheck == 0 && wait_expired(t0, i)) return false;
   }
 }
 
