@@ -1038,8 +1038,14 @@ static cudaError_t plan_launch(TcParams &p, int max_nb_pass, const TcRingPlan &p
   while (raw < kMaxRaw && smem_plan(stages, wslots, raw + 1, max_nb_pass).total + 1024 <= smem_limit && want_r <= 0)
     ++raw;
   while (raw > 2 && smem_plan(stages, wslots, raw, max_nb_pass).total + 1024 > smem_limit) --raw;
+  // Two groups take alternate sequences, and raw slot k % R serves sequences
+  // k and k - R: an odd R gives them to different groups, and the group with
+  // k can reach its raw_full parity wait while k - R's copy has not landed,
+  // when the wait (one phase early) returns at once.  An even R keeps every
+  // raw slot with one group, which takes its sequences in order.
+  if (groups == 2 && raw % 2 == 1) --raw;
   const int st = groups == 2 ? stages : std::min(stages, wslots);
-  if (groups == 2 && wslots > st) return cudaErrorInvalidValue;
+  if (groups == 2 && (wslots > st || raw < 2)) return cudaErrorInvalidValue;
   p.max_nb_pass = max_nb_pass;
   p.stages = st;
   p.wslots = wslots;
