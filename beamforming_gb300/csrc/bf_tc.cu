@@ -392,10 +392,12 @@ __global__ void __launch_bounds__(Roles<kEpiW, kGroups>::kThreads, kHalf ? 2 : 1
                         tt * kTT, pol_e);
         }
       }
-      if (!ok) {  // let copies already issued land before the CTA exits
-        for (uint32_t k = (issued >= static_cast<uint32_t>(R) ? issued - R : 0); k < issued; ++k)
-          mbar_wait_drain(raw_full(static_cast<int>(k % R)), (k / R) & 1u);
-      }
+      // Let the copies already issued land before the CTA exits.  Also when
+      // this thread saw no error: another role's error can end the consumers
+      // before they waited for the last copies.  On a clean run these waits
+      // return at once.
+      for (uint32_t k = (issued >= static_cast<uint32_t>(R) ? issued - R : 0); k < issued; ++k)
+        mbar_wait_drain(raw_full(static_cast<int>(k % R)), (k / R) & 1u);
     }
   } else if (warp == kWProdWarp) {
     // ------------------------------------------------------------ W producer
@@ -458,12 +460,11 @@ __global__ void __launch_bounds__(Roles<kEpiW, kGroups>::kThreads, kHalf ? 2 : 1
                         pass * 2 * P.nb_pass, f, pol_w);
         }
       }
-      if (!ok) {
-        for (uint32_t k = (it >= static_cast<uint32_t>(SW) ? it - SW : 0); k < it; ++k)
-          mbar_wait_drain(w_full(static_cast<int>(k % SW)), (k / SW) & 1u);
-        for (uint32_t k = (dit >= static_cast<uint32_t>(kDigSlots) ? dit - kDigSlots : 0); k < dit; ++k)
-          mbar_wait_drain(d_full(static_cast<int>(k % kDigSlots)), (k / kDigSlots) & 1u);
-      }
+      // as in the E producer: drain on every exit, not only after an own error
+      for (uint32_t k = (it >= static_cast<uint32_t>(SW) ? it - SW : 0); k < it; ++k)
+        mbar_wait_drain(w_full(static_cast<int>(k % SW)), (k / SW) & 1u);
+      for (uint32_t k = (dit >= static_cast<uint32_t>(kDigSlots) ? dit - kDigSlots : 0); k < dit; ++k)
+        mbar_wait_drain(d_full(static_cast<int>(k % kDigSlots)), (k / kDigSlots) & 1u);
     }
   } else if (warp == kMmaWarp) {
     // ------------------------------------------------------------ MMA issuer

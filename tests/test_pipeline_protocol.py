@@ -54,8 +54,11 @@ class Hazard(AssertionError):
 class Model:
     """One CTA of the kernel over `ntiles` tiles of `nk` K stages."""
 
-    def __init__(self, S, SW, R, groups, nk, ntiles, rng):
+    def __init__(self, S, SW, R, groups, nk, ntiles, rng, drain_always=True):
         self.S, self.SW, self.R, self.G, self.nk, self.nt = S, SW, R, groups, nk, ntiles
+        # the producers drain their copies on every exit (False: only after an
+        # error of their own, which leaves copies landing after the exit)
+        self.drain_always = drain_always
         self.total = ntiles * nk
         self.rng = rng
         fwd = groups > 1
@@ -110,6 +113,7 @@ class Model:
         def land():
             on_land()
             bar.complete_tx(nbytes)
+        land.barrier = bar.name
         self.events.append(land)
 
     def mma(self, reads, write):
@@ -140,10 +144,20 @@ class Model:
         return [c for c in self.commits if c[1] <= self.mma_done]
 
     # ------------------------------------------------------------------ roles
+    # A role yields ("wait", barrier, phase) and receives True when the phase
+    # completed, or False when the wait gave up (the kernel's bounded wait:
+    # its own time limit, or another role's error seen in the error word);
+    # ("drain", barrier, phase) ignores the error word, as the kernel's
+    # mbar_wait_drain does.
     def e_producer(self):
+        issued = 0
+        ok = True
         for k in range(self.total):
             r = k % self.R
-            yield self.wait(self.raw_empty[r], k // self.R - 1) if k >= self.R else ("go",)
+            if k >= self.R:
+                ok = yield self.wait(self.raw_empty[r], k // self.R - 1)
+                if not ok:
+                    break
             prev = self.raw[r]
             if prev is not None and prev != (("consumed", k - self.R), True):
                 raise Hazard(f"E producer overwrites raw[{r}] holding {prev} for sequence {k}")
@@ -153,13 +167,22 @@ class Model:
                 self.raw[r] = (k, True)
             self.raw_full[r].arrive(expect_tx=1)
             self.tma(self.raw_full[r], 1, land)
+            issued += 1
+        # let the copies already issued land before the CTA exits, also when
+        # this role saw no error (another role's error can end the consumers)
+        if self.drain_always or not ok:
+            for q in range(max(0, issued - self.R), issued):
+                yield ("drain", self.raw_full[q % self.R], q // self.R)
 
     def w_producer(self):
-        k = 0
+        k = dit = 0
+        ok = True
         for t in range(self.nt):
             d = t % 2
             if t >= 2:
-                yield self.wait(self.d_empty[d], t // 2 - 1)
+                ok = yield self.wait(self.d_empty[d], t // 2 - 1)
+                if not ok:
+                    break
             if self.busy("dslot", d):
                 raise Hazard(f"digits for tile {t} overwrite a slot the tensor core reads")
             self.dslot[d] = (t, False)
@@ -168,14 +191,17 @@ class Model:
                 self.dslot[d] = (t, True)
             self.d_full[d].arrive(expect_tx=1)
             self.tma(self.d_full[d], 1, dland)
+            dit += 1
             for _ in range(self.nk):
                 s = k % self.SW
                 if self.fwd:
                     if k >= self.SW:
                         j = k - self.SW
-                        yield self.wait(self.empty[j % self.S], j // self.S)
+                        ok = yield self.wait(self.empty[j % self.S], j // self.S)
                 elif k >= self.SW:
-                    yield self.wait(self.w_empty[s], k // self.SW - 1)
+                    ok = yield self.wait(self.w_empty[s], k // self.SW - 1)
+                if not ok:
+                    break
                 if self.busy("wslot", s):
                     raise Hazard(f"W producer overwrites W slot {s} for sequence {k} while the tensor core reads it")
                 self.wslot[s] = (k, False)
@@ -185,24 +211,33 @@ class Model:
                 self.w_full[s].arrive(expect_tx=1)
                 self.tma(self.w_full[s], 1, wland)
                 k += 1
+            if not ok:
+                break
+        if self.drain_always or not ok:
+            for q in range(max(0, k - self.SW), k):
+                yield ("drain", self.w_full[q % self.SW], q // self.SW)
+            for q in range(max(0, dit - 2), dit):
+                yield ("drain", self.d_full[q % 2], q // 2)
 
     def forwarder(self):
         for k in range(self.total):
-            yield self.wait(self.w_full[k % self.SW], k // self.SW)
-            if k >= self.S:
-                yield self.wait(self.a_full[(k - self.S) % self.S], (k - self.S) // self.S)
+            if not (yield self.wait(self.w_full[k % self.SW], k // self.SW)):
+                return
+            if k >= self.S and not (yield self.wait(self.a_full[(k - self.S) % self.S], (k - self.S) // self.S)):
+                return
             self.a_full[k % self.S].arrive()
 
     def unpack(self, g):
         for k in range(g, self.total, self.G):
             r, s = k % self.R, k % self.S
-            yield self.wait(self.raw_full[r], k // self.R)
+            if not (yield self.wait(self.raw_full[r], k // self.R)):
+                return
             if self.raw[r] != (k, True):
                 raise Hazard(f"unpack of sequence {k} reads raw[{r}] holding {self.raw[r]}")
             self.raw[r] = (("consumed", k), True)
             self.raw_empty[r].arrive()
-            if k >= self.S:
-                yield self.wait(self.empty[s], k // self.S - 1)
+            if k >= self.S and not (yield self.wait(self.empty[s], k // self.S - 1)):
+                return
             if self.busy("stage", s):
                 raise Hazard(f"unpack of sequence {k} writes TMEM stage {s} while the tensor core reads it")
             self.stage[s] = (k, True)
@@ -210,7 +245,8 @@ class Model:
                 # one group: hand back the W slot of sequence k - S, wait for this one's
                 if k >= self.S:
                     self.w_empty[(k - self.S) % self.SW].arrive()
-                yield self.wait(self.w_full[k % self.SW], k // self.SW)
+                if not (yield self.wait(self.w_full[k % self.SW], k // self.SW)):
+                    return
             self.a_full[s].arrive()
 
     def mma_thread(self):
@@ -218,87 +254,112 @@ class Model:
         nstage = ndig = nacc = 0
         for t in range(self.nt):
             ab = t % 2
-            if t >= 2:
-                yield self.wait(self.accempty[ab], t // 2 - 1)
-            yield self.wait(self.d_full[ab], t // 2)
+            if t >= 2 and not (yield self.wait(self.accempty[ab], t // 2 - 1)):
+                break
+            if not (yield self.wait(self.d_full[ab], t // 2)):
+                break
             if self.acc[ab] is not None and self.acc[ab][0] != t - 2:
                 raise Hazard(f"tile {t} starts accumulator {ab} holding {self.acc[ab]}")
             self.acc[ab] = (t, True)
             self.mma([("dslot", ab, t)], t)
             self.commit(self.d_empty[ab])
             ndig += 1
+            ok = True
             for _ in range(self.nk):
                 s, sw = k % self.S, k % self.SW
-                yield self.wait(self.a_full[s], k // self.S)
+                ok = yield self.wait(self.a_full[s], k // self.S)
+                if not ok:
+                    break
                 self.mma([("stage", s, k), ("wslot", sw, k)], t)
                 self.commit(self.empty[s])
                 nstage += 1
                 k += 1
+            if not ok:
+                break
             self.commit(self.accfull[ab])
             nacc += 1
         # exit drain: the last phase committed on every barrier
         for q in range(max(0, nstage - self.S), nstage):
-            yield self.wait(self.empty[q % self.S], q // self.S)
+            yield ("drain", self.empty[q % self.S], q // self.S)
         for q in range(max(0, ndig - 2), ndig):
-            yield self.wait(self.d_empty[q % 2], q // 2)
+            yield ("drain", self.d_empty[q % 2], q // 2)
         for q in range(max(0, nacc - 2), nacc):
-            yield self.wait(self.accfull[q % 2], q // 2)
+            yield ("drain", self.accfull[q % 2], q // 2)
 
     def epilogue(self):
         for t in range(self.nt):
             ab = t % 2
-            yield self.wait(self.accfull[ab], t // 2)
+            if not (yield self.wait(self.accfull[ab], t // 2)):
+                return
             if self.acc_tile_done.get(t, 0) != 1 + self.nk:
                 raise Hazard(f"epilogue reads tile {t} with {self.acc_tile_done.get(t, 0)} of {1 + self.nk} MMAs done")
             self.accempty[ab].arrive()
 
     # -------------------------------------------------------------- scheduler
-    def run(self, inorder_commits=True):
+    def run(self, inorder_commits=True, fail=None):
+        """Runs every role to its end.  `fail` = (role, n): that role's n-th wait
+        gives up (its time limit), setting the error word; the other roles then
+        give up at any later poll of a wait, as the kernel's do."""
         roles = {"E": self.e_producer(), "W": self.w_producer(), "MMA": self.mma_thread(), "epi": self.epilogue()}
         for g in range(self.G):
             roles[f"unpack{g}"] = self.unpack(g)
         if self.fwd:
             roles["fwd"] = self.forwarder()
         blocked = {name: None for name in roles}
+        nwaits = {name: 0 for name in roles}
         done = set()
+        err = [False]
 
-        def step(name):
+        def resume(name, value):
             gen = roles[name]
-            while True:
+            try:
+                op = gen.send(value) if value is not None else next(gen)
+            except StopIteration:
+                done.add(name)
+                blocked[name] = None
+                return
+            blocked[name] = op
+            settle(name)
+
+        def settle(name):
+            # run a role on while its waits are already decided
+            while name not in done:
                 op = blocked[name]
-                if op is None:
-                    try:
-                        op = next(gen)
-                    except StopIteration:
-                        done.add(name)
+                kind, bar, phase = op
+                if kind == "wait":
+                    nwaits[name] += 1
+                    if fail == (name, nwaits[name]):
+                        err[0] = True
+                        resume(name, False)
                         return
-                if op[0] == "go":
-                    blocked[name] = None
-                    continue
-                _, bar, phase = op
                 if self.check_wait(bar, phase):
-                    blocked[name] = None
-                    continue
-                blocked[name] = op
+                    resume(name, True)
+                    return
                 return
 
         for name in list(roles):
-            step(name)
+            resume(name, None)
         while len(done) < len(roles):
-            runnable = [n for n in roles if n not in done and (blocked[n] is None or
-                                                               self.check_wait(blocked[n][1], blocked[n][2]))]
-            choices = [("role", n) for n in runnable]
-            choices += [("event", i) for i in range(len(self.events))]
+            choices = []
+            for n in roles:
+                if n in done:
+                    continue
+                kind, bar, phase = blocked[n]
+                if self.check_wait(bar, phase):
+                    choices.append(("role", n, True))
+                elif kind == "wait" and err[0]:
+                    choices.append(("role", n, False))  # gives up at a poll of the error word
+            choices += [("event", i, None) for i in range(len(self.events))]
             if self.mma_queue:
-                choices.append(("mma", 0))
+                choices.append(("mma", 0, None))
             dc = self.deliverable_commits()
             if dc:
-                choices += [("commit", i) for i in range(1 if inorder_commits else len(dc))]
+                choices += [("commit", i, None) for i in range(1 if inorder_commits else len(dc))]
             if not choices:
                 raise Hazard(f"deadlock: blocked {[(n, blocked[n][1].name, blocked[n][2]) for n in roles if n not in done]}")
-            kind, i = self.rng.choice(choices)
+            kind, i, val = self.rng.choice(choices)
             if kind == "role":
-                step(i)
+                resume(i, val)
             elif kind == "event":
                 self.events.pop(i)()
             elif kind == "mma":
@@ -307,9 +368,12 @@ class Model:
                 bar, _ = dc[i]
                 self.commits.remove(dc[i])
                 bar.arrive()
-        assert not self.events and not self.mma_queue
-        # every commit's arrival landed before the CTA's exit
+        # nothing asynchronous may land after the CTA exits: every copy landed,
+        # every MMA finished, every commit's arrival delivered
+        assert not self.events, f"copies still to land at exit: {[e.barrier for e in self.events]}"
+        assert not self.mma_queue, f"{len(self.mma_queue)} MMAs still running at exit"
         assert not self.commits, f"commits still to land at exit: {[c[0].name for c in self.commits]}"
+        return err[0]
 
 
 # The layouts the planner produces: S stages, SW W slots, R raw slots, unpack groups.
@@ -332,6 +396,37 @@ def test_protocol_random_schedules(name, inorder):
     for seed in range(150):
         rng = random.Random(hash((name, inorder, seed)) & 0xFFFFFFFF)
         Model(ntiles=7, rng=rng, **cfg).run(inorder_commits=inorder)
+
+
+@pytest.mark.parametrize("name", sorted(LAYOUTS))
+def test_protocol_error_paths(name):
+    """One role's wait gives up at a random point (its time limit); the others
+    give up at later polls and drain: no deadlock, no hazard, and nothing
+    asynchronous left to land after the CTA exits."""
+    cfg = LAYOUTS[name]
+    roles = ["E", "W", "MMA", "epi", "unpack0"] + (["unpack1", "fwd"] if cfg["groups"] > 1 else [])
+    failed = 0
+    for seed in range(150):
+        rng = random.Random(hash((name, "fail", seed)) & 0xFFFFFFFF)
+        fail = (rng.choice(roles), rng.randint(1, 12))
+        failed += Model(ntiles=5, rng=rng, **cfg).run(inorder_commits=bool(seed % 2), fail=fail)
+    assert failed > 50  # most injections hit a wait that happened
+
+
+def test_protocol_model_finds_producers_that_drain_only_on_own_errors():
+    """With the producers draining only after an error of their own, some
+    injected failure leaves a copy landing after the CTA exits."""
+    found = False
+    for seed in range(300):
+        rng = random.Random(seed)
+        fail = (rng.choice(["MMA", "unpack0", "unpack1", "fwd", "epi"]), rng.randint(1, 12))
+        try:
+            Model(ntiles=5, rng=rng, drain_always=False, **LAYOUTS["b32 two groups"]).run(fail=fail)
+        except AssertionError as e:
+            assert "still to land" in str(e)
+            found = True
+            break
+    assert found
 
 
 def test_protocol_model_finds_odd_raw_rings_with_two_groups():
