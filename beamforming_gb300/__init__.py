@@ -36,7 +36,7 @@ ERR_TOO_LARGE = 9
 PTR_HOST = 0
 PTR_DEVICE = 1
 
-KERNELS = {"auto": 0, "tensor": 1, "simt": 2}
+KERNELS = {"auto": 0, "tensor": 1, "simt": 2, "simt4": 3}
 
 # Every symbol the C header declares; the CPU tests check the library exports them.
 EXPORTED_SYMBOLS = (

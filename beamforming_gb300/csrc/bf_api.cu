@@ -101,6 +101,8 @@ std::atomic<int> g_kernel{BF_KERNEL_AUTO};
 thread_local int t_last_status = BF_OK;
 thread_local const char *t_last_kernel = "none";
 
+const char *simt_name() { return g_kernel.load() == BF_KERNEL_SIMT4 ? "simt4" : "simt"; }
+
 bool dims_valid(const bf_dims *d) {
   return d && d->ntimes >= 0 && d->nfrequencies >= 0 && d->ndishes >= 0 && d->npolarizations >= 0 &&
          d->nbeams >= 0;
@@ -132,7 +134,8 @@ int choose_tensor(const bf_dims &d, bool *use_tc) {
   const int k = g_kernel.load();
   const bool ok = tc_supported(d);
   if (k == BF_KERNEL_TENSOR && !ok) return BF_ERR_UNSUPPORTED;
-  if (k == BF_KERNEL_SIMT && (d.npolarizations < 1 || d.npolarizations > 2)) return BF_ERR_UNSUPPORTED;
+  if ((k == BF_KERNEL_SIMT || k == BF_KERNEL_SIMT4) && (d.npolarizations < 1 || d.npolarizations > 2))
+    return BF_ERR_UNSUPPORTED;
   if (k == BF_KERNEL_AUTO && !ok && (d.npolarizations < 1 || d.npolarizations > 2)) return BF_ERR_UNSUPPORTED;
   *use_tc = (k == BF_KERNEL_TENSOR) || (k == BF_KERNEL_AUTO && ok);
   return BF_OK;
@@ -165,7 +168,7 @@ int run_device_bufs(const bf_dims &d, uint8_t *J, const uint8_t *E, const uint8_
     use_tc = false;
   }
   if (!use_tc) {
-    t_last_kernel = "simt";
+    t_last_kernel = simt_name();
     return to_status(launch_simt(d, J, E, A, G, s, 0, a_layout, j_layout));
   }
   TcWeights w;
@@ -300,7 +303,7 @@ int run_host_pipelined(DeviceCtx &c, const bf_dims &d, uint8_t *J, const uint8_t
   }
   BF_TRY(cudaEventRecord(l0.done, l0.s));
   for (int i = 1; i < kLanes; ++i) BF_TRY(cudaStreamWaitEvent(c.lanes[i].s, l0.done, 0));
-  t_last_kernel = use_tc ? "tensor" : "simt";
+  t_last_kernel = use_tc ? "tensor" : simt_name();
   uint8_t *jmap = mapped_host_j(J, d, j_layout);
   const int64_t P = d.npolarizations;
   const int64_t jrows = j_layout == kJ2 ? d.nbeams * d.nfrequencies : d.nbeams * d.nfrequencies * P;
@@ -335,6 +338,8 @@ int run_host_pipelined(DeviceCtx &c, const bf_dims &d, uint8_t *J, const uint8_t
 }
 
 }  // namespace
+
+bool simt_four_multiply() { return g_kernel.load() == BF_KERNEL_SIMT4; }
 
 int device_error_word(int **out) {
   DeviceCtx *c = nullptr;
@@ -384,7 +389,7 @@ const char *bf_status_string(int status) {
 }
 
 int bf_set_kernel(int kernel) {
-  if (kernel < BF_KERNEL_AUTO || kernel > BF_KERNEL_SIMT) return BF_ERR_INVALID_ARGUMENT;
+  if (kernel < BF_KERNEL_AUTO || kernel > BF_KERNEL_SIMT4) return BF_ERR_INVALID_ARGUMENT;
   g_kernel.store(kernel);
   return BF_OK;
 }
@@ -600,7 +605,7 @@ int bf_form_beams_resident(const bf_weights *w, int64_t ntimes, uint8_t *J, cons
     t_last_kernel = "tensor";
     return to_status(launch_tc(w->tc, ntimes, J, E, c->err, s));
   }
-  t_last_kernel = "simt";
+  t_last_kernel = simt_name();
   return to_status(launch_simt(d, J, E, w->A, w->G, s));
 }
 

@@ -61,6 +61,10 @@ __device__ __forceinline__ void load_a(const uint8_t *A, int a_layout, int64_t f
 }
 #endif
 
+// True while bf_set_kernel(BF_KERNEL_SIMT4) selects the 4-multiply SIMT
+// kernel; otherwise launch_simt runs the Gauss 3-multiply kernel.
+bool simt_four_multiply();
+
 // Exact integer SIMT kernel (dp4a); any shape with npolarizations <= 2.  J
 // rows (b, f, p) -- (b, f) for J2 -- are `jpitch` (2 * jpitch for J2) bytes
 // apart (0: ntimes).

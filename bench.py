@@ -66,11 +66,12 @@ def parse_args():
     ap.add_argument("--times", type=int, default=None, help="override t (profiling)")
     ap.add_argument(
         "--workload",
-        choices=["chunk", "batched", "served", "wide"],
+        choices=["chunk", "batched", "served", "wide", "exact"],
         default="chunk",
         help="chunk: the full single-GPU chunk (default); batched: 128 uneven problems in one persistent launch; "
         "served: the Poisson chunk stream through the continuous-batching server against the plain loop; "
-        "wide: d=1024 b=512 chunks through the server with weight refresh every 8 chunks",
+        "wide: d=1024 b=512 chunks through the server with weight refresh every 8 chunks; "
+        "exact: the exact dp4a kernel's Gauss and 4-multiply forms on the full chunk",
     )
     ap.add_argument("--chunks", type=int, default=64, help="wide: chunks per round of the timed served loop")
     ap.add_argument("--rounds", type=int, default=6, help="wide: rounds (J checked between rounds)")
@@ -751,6 +752,62 @@ def other_workloads(args):
         "kernel_roofline_frac": w["roofline"]["frac"], "roofline_bound": w["roofline"]["bound"],
         "kernel_ms": w["roofline"].get("kernel_ms"), "weight_updates": w["served"]["weight_updates"],
         "mismatches": w["mismatches"], "clocks": w.get("clocks")}
+    try:
+        out["exact_fallback"] = run_exact_forms()
+    except Exception as e:  # the headline line must still print
+        out["exact_fallback"] = {"error": f"{type(e).__name__}: {e}"}
+    return out
+
+
+def run_exact_forms(reps=3):
+    """The exact dp4a kernel (the fallback for shapes the tensor-core kernel
+    does not take) on the full chunk in both of its forms: the Gauss
+    3-multiply form (the default) and the reference's 4-multiply form.  CUDA
+    events around each launch after one warm-up; J's adler32 must equal the
+    tensor-core kernel's (and the reference cpu.cxx's, where the golden holds
+    it)."""
+    import torch
+
+    import beamforming_gb300 as bf
+
+    d = dims()
+    seed = WORKLOAD["seed"]
+    E = torch.empty(d.esize, dtype=torch.uint8, device="cuda")
+    A = torch.empty(d.asize, dtype=torch.uint8, device="cuda")
+    bf.fill_random_device(E, seed, 0)
+    bf.fill_random_device(A, seed, 1)
+    G = torch.from_numpy(bf.gains(d)).cuda()
+    J = torch.empty(d.jsize, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    bf.set_kernel("tensor")
+    try:
+        bf.form_beams_ex(d, J, E, A, G, stream=stream)
+        bf.stream_status(stream)
+        want = bf.adler32_device(J)
+        out = {"workload": WORKLOAD_NAME, "unit": "complex beam-MACs/s", "reps": reps}
+        for name, kernel in (("gauss", "simt"), ("four_multiply", "simt4")):
+            bf.set_kernel(kernel)
+            J.fill_(0x5A)
+            bf.form_beams_ex(d, J, E, A, G, stream=stream)
+            bf.stream_status(stream)
+            ok = bf.adler32_device(J) == want
+            evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+            for a, b in evs:
+                a.record(stream)
+                bf.form_beams_ex(d, J, E, A, G, stream=stream)
+                b.record(stream)
+            torch.cuda.synchronize()
+            bf.stream_status(stream)
+            ms = statistics.mean(a.elapsed_time(b) for a, b in evs)
+            out[name] = {"ms": round(ms, 3), "value": d.cmacs / (ms * 1e-3), "adler32_equals_tensor": ok}
+    finally:
+        bf.set_kernel("auto")
+    golden = golden_full_adler32()
+    out["adler32"] = f"{want:#010x}"
+    out["adler32_equals_reference_cpu"] = None if golden is None else want == golden
+    out["gauss_speedup"] = round(out["four_multiply"]["ms"] / out["gauss"]["ms"], 3)
+    del E, A, J
+    torch.cuda.empty_cache()
     return out
 
 
@@ -1322,7 +1379,9 @@ def main():
     if args.times:
         WORKLOAD["ntimes"] = args.times
         WORKLOAD_NAME = WORKLOAD_NAME.replace("t=32768", f"t={args.times}")
-    if args.profile_kernel:
+    if args.workload == "exact":
+        print(json.dumps(run_exact_forms(reps=max(3, args.steps))), flush=True)
+    elif args.profile_kernel:
         profile_kernel(args)
     elif args.impl == "reference" and args.reference_kernel:
         run_reference_kernel(args)

@@ -76,7 +76,8 @@ typedef enum bf_ptr_kind { BF_PTR_HOST = 0, BF_PTR_DEVICE = 1 } bf_ptr_kind;
 typedef enum bf_kernel {
   BF_KERNEL_AUTO = 0,   /* tensor-core kernel where the shape allows, else SIMT */
   BF_KERNEL_TENSOR = 1, /* tcgen05 tensor-core kernel (fails if the shape does not fit) */
-  BF_KERNEL_SIMT = 2    /* exact integer dp4a kernel, any shape */
+  BF_KERNEL_SIMT = 2,   /* exact integer dp4a kernel, any shape (Gauss 3-multiply form) */
+  BF_KERNEL_SIMT4 = 3   /* the same with the reference's 4-multiply form (cpu.cxx:33-34) */
 } bf_kernel;
 
 /* ------------------------------------------------------------------ drop-in */

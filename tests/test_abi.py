@@ -63,6 +63,9 @@ def test_invalid_arguments(bflib):
     assert L.bf_set_dims(ctypes.byref(d)) == bflib.ERR_INVALID_ARGUMENT
     assert L.bf_set_dims(None) == bflib.ERR_INVALID_ARGUMENT
     assert L.bf_set_kernel(7) == bflib.ERR_INVALID_ARGUMENT
+    assert L.bf_set_kernel(4) == bflib.ERR_INVALID_ARGUMENT
+    assert L.bf_set_kernel(3) == 0  # the 4-multiply SIMT form
+    assert L.bf_set_kernel(0) == 0
     d = bflib.Dims(4, 1, 8, 2, 8).c()
     assert L.bf_form_beams_ex(ctypes.byref(d), None, None, None, None, 0, None) == bflib.ERR_INVALID_ARGUMENT
     J = np.zeros(64, np.uint8)

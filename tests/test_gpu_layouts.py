@@ -21,7 +21,7 @@ def _inputs(bflib, T, F, D, B, seed):
     return d, E, A, bflib.gains(d)
 
 
-@pytest.mark.parametrize("kernel", ["tensor", "simt"])
+@pytest.mark.parametrize("kernel", ["tensor", "simt", "simt4"])
 @pytest.mark.parametrize("shape", SHAPES)
 def test_layouts_match_oracle(bflib, oracle, kernel, shape):
     d, E, A, G = _inputs(bflib, *shape, seed=sum(shape))

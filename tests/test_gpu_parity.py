@@ -78,7 +78,7 @@ def test_random_shapes_tensor_vs_oracle(bflib, cuda, oracle, shape):
 
 
 @pytest.mark.parametrize("shape", TC_SHAPES)
-@pytest.mark.parametrize("kernel", ["tensor", "simt"])
+@pytest.mark.parametrize("kernel", ["tensor", "simt", "simt4"])
 def test_seeded_shapes_match_oracle(bflib, cuda, oracle, shape, kernel):
     d = bflib.Dims(*shape)
     E, A, G = bflib.seeded_host_inputs(d, 100 + sum(shape))
@@ -98,7 +98,11 @@ def test_odd_shapes_auto_dispatch(bflib, cuda, oracle, shape):
     E, A, G = bflib.seeded_host_inputs(d, 7)
     J = run_gpu(bflib, cuda, d, E, A, G, "auto")
     assert bflib.last_kernel() == "simt"
-    np.testing.assert_array_equal(J, oracle.form_beams(oracle_dims(oracle, d), E, A, G))
+    want = oracle.form_beams(oracle_dims(oracle, d), E, A, G)
+    np.testing.assert_array_equal(J, want)
+    J4 = run_gpu(bflib, cuda, d, E, A, G, "simt4")  # the 4-multiply form
+    assert bflib.last_kernel() == "simt4"
+    np.testing.assert_array_equal(J4, want)
 
 
 def test_tensor_kernel_refuses_odd_shape(bflib, cuda):
@@ -222,7 +226,7 @@ def test_adversarial_extremes(bflib, cuda, oracle, kind, D):
     base = np.float32(7.5 / (2 * 64 * D))
     G = (rng.uniform(-2, 2, d.gsize).astype(np.float32) * base).astype(np.float32)
     G[0], G[1], G[2] = 0.0, np.float32(0.5 / 128), np.float32(-1.5 / 256)
-    for kernel in ("tensor", "simt"):
+    for kernel in ("tensor", "simt", "simt4"):
         J = run_gpu(bflib, cuda, d, E, A, G, kernel)
         np.testing.assert_array_equal(J, oracle.form_beams(oracle_dims(oracle, d), E, A, G), err_msg=kernel)
 
@@ -232,7 +236,7 @@ def test_half_way_rounding(bflib, cuda, oracle):
     d = bflib.Dims(64, 1, 64, 2, 16)
     E, A, G = bflib.seeded_host_inputs(d, 3)
     G[:] = np.float32(0.5) ** np.arange(1, 17, dtype=np.float32)
-    for kernel in ("tensor", "simt"):
+    for kernel in ("tensor", "simt", "simt4"):
         J = run_gpu(bflib, cuda, d, E, A, G, kernel)
         np.testing.assert_array_equal(J, oracle.form_beams(oracle_dims(oracle, d), E, A, G), err_msg=kernel)
 
@@ -246,7 +250,7 @@ def test_gain_ranges(bflib, cuda, oracle, scale):
     rng = np.random.default_rng(int(scale * 10) + 1)
     G = (rng.uniform(-1, 1, d.gsize) * scale).astype(np.float32)
     G[::7] = np.float32(0.0)
-    for kernel in ("tensor", "simt"):
+    for kernel in ("tensor", "simt", "simt4"):
         J = run_gpu(bflib, cuda, d, E, A, G, kernel)
         np.testing.assert_array_equal(J, oracle.form_beams(oracle_dims(oracle, d), E, A, G), err_msg=kernel)
 
@@ -447,3 +451,28 @@ def test_device_wait_timeout_reports_and_recovers(bflib, cuda, oracle, B):
         bflib.set_test_stall(False)
     J = run_gpu(bflib, cuda, d, E, A, G, "tensor")
     np.testing.assert_array_equal(J, oracle.form_beams(oracle_dims(oracle, d), E, A, G))
+
+
+@pytest.mark.parametrize("shape", [(96, 2, 64, 2, 40), (64, 1, 128, 1, 33)])
+def test_unaligned_operands_take_the_byte_path(bflib, cuda, oracle, shape):
+    """E and A one byte off a 4-byte boundary (D % 4 == 0): the exact kernel
+    decodes byte by byte instead of by words; auto dispatch goes there too."""
+    d = bflib.Dims(*shape)
+    E, A, G = bflib.seeded_host_inputs(d, 31)
+    want = oracle.form_beams(oracle_dims(oracle, d), E, A, G)
+    Eb = cuda.zeros(d.esize + 16, dtype=cuda.uint8, device="cuda")
+    Ab = cuda.zeros(d.asize + 16, dtype=cuda.uint8, device="cuda")
+    Ed, Ad = Eb[1:1 + d.esize], Ab[3:3 + d.asize]
+    Ed.copy_(cuda.from_numpy(E))
+    Ad.copy_(cuda.from_numpy(A))
+    assert Ed.data_ptr() % 4 and Ad.data_ptr() % 4
+    Gd = _dev(cuda, G)
+    for kernel in ("simt", "simt4", "auto"):
+        bflib.set_kernel(kernel)
+        try:
+            Jd = cuda.full((d.jsize,), 0x5A, dtype=cuda.uint8, device="cuda")
+            bflib.form_beams_ex(d, Jd, Ed, Ad, Gd)
+            bflib.stream_status()
+        finally:
+            bflib.set_kernel("auto")
+        np.testing.assert_array_equal(Jd.cpu().numpy(), want, err_msg=kernel)
