@@ -48,6 +48,7 @@ EXPORTED_SYMBOLS = (
     "bf_form_beams_ex",
     "bf_stream_status",
     "bf_set_kernel",
+    "bf_plan_rings",
     "bf_set_test_stall",
     "bf_last_kernel",
     "bf_weights_create",
@@ -157,6 +158,8 @@ def lib() -> ctypes.CDLL:
                                           ctypes.POINTER(ctypes.c_uint32), vp]
         L.bf_stream_status.argtypes = [vp]
         L.bf_set_kernel.argtypes = [ctypes.c_int]
+        L.bf_plan_rings.argtypes = [ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                    ctypes.POINTER(ctypes.c_int)]
         L.bf_set_test_stall.argtypes = [ctypes.c_int]
         L.bf_last_kernel.argtypes = []
         L.bf_last_kernel.restype = ctypes.c_char_p
@@ -337,6 +340,16 @@ def form_beams_adler(dims: Dims, J, E, A, G, a_layout: str = "linear", j_layout:
 def stream_status(stream=None) -> None:
     """Synchronizes the stream and raises if a kernel reported an error."""
     _check(lib().bf_stream_status(_stream_handle(stream)), "bf_stream_status")
+
+
+def plan_rings(ndishes: int, max_nb_pass: int, wslots: int = 0, raw: int = 0) -> dict | None:
+    """The ring layout the tensor-core kernel plans (host only, no GPU), or
+    None where no layout fits: TMEM stages, W slots, raw E slots, unpack
+    groups, CTAs per SM and K stages per tile."""
+    out = (ctypes.c_int * 6)()
+    if lib().bf_plan_rings(ndishes, max_nb_pass, wslots, raw, out) != 0:
+        return None
+    return dict(zip(("stages", "wslots", "raw", "groups", "ctas_per_sm", "nk"), list(out)))
 
 
 def set_kernel(kind: str) -> None:

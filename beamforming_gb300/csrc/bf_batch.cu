@@ -243,6 +243,15 @@ int bf_batch_info(const bf_batch *b, int *ntiles, int *order, int *wslots, int *
   return BF_OK;
 }
 
+int bf_plan_rings(int64_t ndishes, int max_nb_pass, int wslots, int raw, int *out) {
+  if (!out || ndishes <= 0 || ndishes > 2048 || max_nb_pass <= 0 || max_nb_pass > 128 || wslots < 0 || raw < 0)
+    return BF_ERR_INVALID_ARGUMENT;
+  bf::TcRingPlan plan;
+  plan.wslots = wslots;
+  plan.raw = raw;
+  return bf::tc_plan_rings(ndishes, max_nb_pass, plan, out) == cudaSuccess ? BF_OK : BF_ERR_INVALID_ARGUMENT;
+}
+
 int bf_batch_shape(const bf_batch *b, int *nlaunches, int *nproblems, int *ntiles, int *max_nb_pass, int *stages,
                    int *unpack_groups, int *ctas_per_sm) {
   if (!b || !nlaunches) return BF_ERR_INVALID_ARGUMENT;

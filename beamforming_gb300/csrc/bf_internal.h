@@ -172,6 +172,10 @@ int tc_stages_per_tile(int64_t D);
 cudaError_t launch_tc_grouped(const TcProblem *table, int nprob, int ntiles, int64_t D, int max_nb_pass,
                               const TcRingPlan &plan, int *err, cudaStream_t s);
 
+// The whole ring layout of a launch with these sizes: out[0..5] = stages,
+// W slots, raw E slots, unpack groups, CTAs per SM, K stages per tile.
+cudaError_t tc_plan_rings(int64_t D, int max_nb_pass, const TcRingPlan &plan, int *out);
+
 // TMEM stages, unpack groups and CTAs per SM of a grouped launch with these sizes.
 cudaError_t tc_launch_shape(int64_t D, int max_nb_pass, const TcRingPlan &plan, int *stages, int *groups,
                             int *ctas_per_sm);

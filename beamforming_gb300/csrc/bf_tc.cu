@@ -1117,6 +1117,21 @@ int64_t tc_problem_tiles(const TcProblem &P) { return static_cast<int64_t>(P.ntt
 
 int tc_stages_per_tile(int64_t D) { return static_cast<int>((D + kStageK / 2 - 1) / (kStageK / 2)); }
 
+cudaError_t tc_plan_rings(int64_t D, int max_nb_pass, const TcRingPlan &plan, int *out) {
+  TcParams p{};
+  p.nk = tc_stages_per_tile(D);
+  int smem_bytes = 0;
+  const cudaError_t e = plan_launch(p, max_nb_pass, plan, &smem_bytes);
+  if (e != cudaSuccess) return e;
+  out[0] = p.stages;
+  out[1] = p.wslots;
+  out[2] = p.raw;
+  out[3] = p.groups;
+  out[4] = p.half ? 2 : 1;
+  out[5] = p.nk;
+  return cudaSuccess;
+}
+
 cudaError_t tc_launch_shape(int64_t D, int max_nb_pass, const TcRingPlan &plan, int *stages, int *groups,
                             int *ctas_per_sm) {
   TcParams p{};

@@ -190,6 +190,15 @@ BF_API int bf_batch_shape(const bf_batch *batch, int *nlaunches, int *nproblems,
 
 BF_API int bf_batch_destroy(bf_batch *batch);
 
+/* The ring layout the tensor-core kernel plans for a launch over ndishes
+ * dishes whose widest beam pass has max_nb_pass beams, with wslots W slots
+ * and raw raw-E slots asked for (0: the planner's choice).  out[0..5] =
+ * unpacked stages in tensor memory, W slots, raw E slots, unpack warp
+ * groups, CTAs per SM, K stages per tile.  Host only: needs no GPU.
+ * BF_ERR_INVALID_ARGUMENT where no layout fits.  No counterpart in the
+ * reference. */
+BF_API int bf_plan_rings(int64_t ndishes, int max_nb_pass, int wslots, int raw, int *out);
+
 /* Array layouts (for bf_form_beams_layout).  BF_A_LINEAR / BF_J_LINEAR are the
  * reference's A[f][b][d] and J[b][f][p][t] (Alinear, Jlinear; arraysizes.hxx:92,
  * 115) used everywhere else in this API.  BF_A_A2 is the lossy kernel family's

@@ -18,8 +18,14 @@ content still in use, a parity wait that could alias a phase, and deadlock.
 from __future__ import annotations
 
 import random
+import zlib
 
 import pytest
+
+
+def _seed(*parts):
+    """A reproducible seed (str hashes change from process to process)."""
+    return zlib.crc32("|".join(map(str, parts)).encode())
 
 
 class Barrier:
@@ -394,7 +400,7 @@ def test_protocol_random_schedules(name, inorder):
     """No deadlock, no hazard and no phase alias over many random schedules."""
     cfg = LAYOUTS[name]
     for seed in range(150):
-        rng = random.Random(hash((name, inorder, seed)) & 0xFFFFFFFF)
+        rng = random.Random(_seed(name, inorder, seed))
         Model(ntiles=7, rng=rng, **cfg).run(inorder_commits=inorder)
 
 
@@ -407,10 +413,52 @@ def test_protocol_error_paths(name):
     roles = ["E", "W", "MMA", "epi", "unpack0"] + (["unpack1", "fwd"] if cfg["groups"] > 1 else [])
     failed = 0
     for seed in range(150):
-        rng = random.Random(hash((name, "fail", seed)) & 0xFFFFFFFF)
+        rng = random.Random(_seed(name, "fail", seed))
         fail = (rng.choice(roles), rng.randint(1, 12))
         failed += Model(ntiles=5, rng=rng, **cfg).run(inorder_commits=bool(seed % 2), fail=fail)
     assert failed > 50  # most injections hit a wait that happened
+
+
+def _planned_layouts(bflib):
+    """Every ring layout the kernel's planner (bf_plan_rings) gives over the
+    dish counts and pass widths it takes and the batch autotuner's three ring
+    plans, with the dish counts that give each."""
+    layouts = {}
+    for D in (8, 64, 128, 192, 512, 1024, 2048):
+        for nb in range(8, 97, 8):
+            for wslots, raw in ((0, 0), (4, 8), (2, 12)):
+                pl = bflib.plan_rings(D, nb, wslots, raw)
+                assert pl is not None, (D, nb, wslots, raw)
+                key = (pl["stages"], pl["wslots"], pl["raw"], pl["groups"])
+                layouts.setdefault(key, set()).add(pl["nk"])
+    return layouts
+
+
+def test_every_planned_layout_passes_the_model(bflib):
+    """The model over every layout the planner produces (not only the ones
+    listed above), with 1, 2, 3 and 8 K stages per tile as well as the
+    planner's own: random schedules with commits in and out of order, and
+    injected failures."""
+    layouts = _planned_layouts(bflib)
+    assert len(layouts) >= 10
+    for (S, SW, R, groups), nks in sorted(layouts.items()):
+        assert groups == 1 or (R % 2 == 0 and SW <= S), (S, SW, R, groups)  # the planner's two-group rules
+        roles = ["E", "W", "MMA", "epi", "unpack0"] + (["unpack1", "fwd"] if groups > 1 else [])
+        for nk in sorted(set(nks) | {1, 2, 3, 8}):
+            cfg = dict(S=S, SW=SW, R=R, groups=groups, nk=min(nk, 8))
+            for seed in range(12):
+                rng = random.Random(_seed(S, SW, R, groups, nk, seed))
+                Model(ntiles=5, rng=rng, **cfg).run(inorder_commits=bool(seed % 2))
+                fail = (rng.choice(roles), rng.randint(1, 12))
+                Model(ntiles=5, rng=rng, **cfg).run(inorder_commits=bool(seed % 2), fail=fail)
+
+
+def test_planner_refuses_passes_it_cannot_hold(bflib):
+    assert bflib.plan_rings(512, 104) is None  # wider than 96 beams: no TMEM room for two stages
+    assert bflib.plan_rings(4096, 96) is None  # beyond the kernel's 2048 dishes
+    assert bflib.plan_rings(512, 16)["ctas_per_sm"] == 2
+    assert bflib.plan_rings(512, 96)["groups"] == 1
+    assert bflib.plan_rings(512, 64)["groups"] == 2
 
 
 def test_protocol_model_finds_producers_that_drain_only_on_own_errors():
