@@ -445,6 +445,7 @@ class Server:
         _check(lib().bf_server_create(ctypes.byref(h), weights._h, ctypes.byref(cfg)), "bf_server_create")
         self._h = h
         self._live: dict[int, tuple] = {}
+        self._replay_keep: list = []  # buffers of a failed replay, held until close()
 
     def submit(self, channel: int, ntimes: int, E, J, nchannels: int = 1) -> int:
         w = self.weights
@@ -508,10 +509,14 @@ class Server:
         wall = ctypes.c_double()
         stalls = ctypes.c_int64()
         dp = ctypes.POINTER(ctypes.c_double)
-        _check(lib().bf_server_replay(
+        rc = lib().bf_server_replay(
             self._h, n, ch, nt, E_arr, ekind, J_arr, len(jptr), jb, jkind, arr, check_threads,
             lat.ctypes.data_as(dp), late.ctypes.data_as(dp), adl.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
-            ctypes.byref(wall), ctypes.byref(stalls)), "bf_server_replay")
+            ctypes.byref(wall), ctypes.byref(stalls))
+        if rc != 0:
+            # chunks already submitted may still be landing: keep their buffers until close()
+            self._replay_keep.append((list(E_list), list(J_slots)))
+        _check(rc, "bf_server_replay")
         return {"latency_s": lat, "late_s": late, "adler32": adl, "wall_s": wall.value, "slot_stalls": stalls.value}
 
     def stats(self) -> dict:

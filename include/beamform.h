@@ -308,7 +308,10 @@ BF_API int bf_server_stats_get(bf_server *server, bf_server_stats *stats);
  * the waits).  late_s[i] (may be NULL) is how late chunk i was submitted.
  * Returns when every chunk is complete and checked, with the time from the
  * call to the last completion in *wall_s.  Checking needs J in host memory.
- * No counterpart in the reference. */
+ * On an error (a failed submission or wait) it returns that status without
+ * submitting more; chunks already submitted may still be landing in their J
+ * slots, so keep E and the J slots alive until bf_server_destroy, which waits
+ * for them.  No counterpart in the reference. */
 BF_API int bf_server_replay(bf_server *server, int n, const int *channel, const int64_t *ntimes,
                             const uint8_t *const *E, int e_on_device, uint8_t *const *J_slots, int nslots,
                             const int64_t *j_bytes, int j_on_device, const double *arrival_s, int check_threads,
