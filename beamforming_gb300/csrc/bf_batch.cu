@@ -98,6 +98,18 @@ Schedule schedule_of(const std::vector<TcProblem> &probs, const std::vector<int>
   return sc;
 }
 
+// The device error word after the tuning launches: a bounded wait that gave
+// up in any candidate voids the timings and the outputs (the word is cleared).
+int take_device_error(int *err, cudaStream_t s) {
+  int h = 0;
+  BF_TRY(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  BF_TRY(cudaStreamSynchronize(s));
+  if (h == 0) return BF_OK;
+  BF_TRY(cudaMemsetAsync(err, 0, sizeof(int), s));
+  BF_TRY(cudaStreamSynchronize(s));
+  return BF_ERR_DEVICE_TIMEOUT;
+}
+
 cudaError_t launch_schedule(const bf_batch *b, const BatchLaunch *ls, int n, const TcRingPlan &plan,
                             cudaStream_t s) {
   for (int i = 0; i < n; ++i) {
@@ -192,6 +204,7 @@ int bf_batch_create(bf_batch **out, const bf_problem *problems, int nproblems, b
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  if (st == BF_OK) st = take_device_error(err, s);
   if (st == BF_OK) {
     const Schedule sc = schedule_of(probs, *orders[b->order], b->cuts);
     b->tuned_ms = best / 3.0f;

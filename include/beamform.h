@@ -164,16 +164,19 @@ typedef struct bf_problem {
 
 /* Builds a batch: times a few launch schedules on the given buffers (tile
  * shape x tile order x shared-memory ring plan), keeps the fastest and
- * captures it in a CUDA graph.  The tile shape is either one persistent
- * launch over every problem, or -- when the batch mixes beam passes wider and
- * narrower than 64 beams -- the narrow ones in a launch of their own, whose
- * smaller accumulators leave tensor memory for four or more unpacked stages
- * and two unpack warp groups.  The buffers must stay allocated while the batch exists; their
- * contents may change between runs.  Each problem needs the tensor-core shape
- * rules (ntimes % 16 == 0, ndishes % 8 == 0, ndishes <= 2048, 16-byte aligned E and J). */
+ * captures it in a CUDA graph.  The tile shape groups the problems by beam
+ * pass width into one to three persistent launches: passes wider than 64
+ * beams; at most 64 (smaller accumulators leave tensor memory for four or
+ * more unpacked stages and two unpack warp groups); at most 16 (two CTAs per
+ * SM).  Classes share a launch unless timing says to split them.  The
+ * buffers must stay allocated while the batch exists; their contents may
+ * change between runs.  Each problem needs the tensor-core shape rules
+ * (ntimes % 16 == 0, ndishes % 8 == 0, ndishes <= 2048, 16-byte aligned E and
+ * J).  BF_ERR_DEVICE_TIMEOUT if a bounded device wait gave up while tuning. */
 BF_API int bf_batch_create(bf_batch **out, const bf_problem *problems, int nproblems, bf_stream_t stream);
 
-/* Runs every problem of the batch once (graph replay); asynchronous on `stream`. */
+/* Runs every problem of the batch once (graph replay); asynchronous on
+ * `stream`.  bf_stream_status(stream) reports a device wait that gave up. */
 BF_API int bf_batch_run(bf_batch *batch, bf_stream_t stream);
 
 /* The schedule the autotuner chose: tiles, tile order (0 as given, 1 largest
