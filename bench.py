@@ -711,51 +711,62 @@ def other_workloads(args):
     """The batched, served and wide workloads in compact form, so that one
     default run records all of them (one GPU): the batched set with every
     problem checked against the oracle, a 10 s served stream plus the
-    back-to-back runs for both loops (every chunk checked), and three rounds
-    of wide-array chunks with weight refresh (every chunk checked).  The full
-    records come from `--workload batched|served|wide`."""
+    back-to-back runs for both loops (every chunk checked), three rounds of
+    wide-array chunks with weight refresh (every chunk checked), and the exact
+    dp4a kernel's two forms on the full chunk.  The full records come from
+    `--workload batched|served|wide|exact`.  A workload that fails is recorded
+    with its error, so that the headline line still prints."""
     import copy
 
+    def batched():
+        a = copy.copy(args)
+        a.steps, a.warmup = 20, 3
+        b = run_batched(a, emit=False)
+        return {
+            "workload": b["config"]["workload"], "value": b["value"], "unit": b["unit"],
+            "ms_per_step": b["ms_per_step"], "roofline_frac": b["roofline"]["frac"],
+            "roofline_bound": b["roofline"]["bound"], "speedup_vs_per_problem": b["speedup_vs_per_problem"],
+            "launches": [(L["problems"], L["max_nb_pass"], L["ctas_per_sm"]) for L in b["autotune"]["launches"]],
+            "parity": b["parity"]}
+
+    def served():
+        a = copy.copy(args)
+        a.duration, a.repeats, a.extra_rates = 10.0, 1, []
+        sv = run_served(a, emit=False)
+
+        def lat(r):
+            return {q: r["latency_ms"][q] for q in ("p50", "p99", "p99.9")}
+
+        return {
+            "workload": sv["config"]["workload"].replace("for 30 s", "for 10 s"), "unit": "beam samples/s",
+            "served": {"latency_ms": lat(sv["served"]), "beam_samples_per_s": sv["served"]["beam_samples_per_s"]},
+            "plain": {"latency_ms": lat(sv["plain_loop"]),
+                      "beam_samples_per_s": sv["plain_loop"]["beam_samples_per_s"]},
+            "saturation": {"served": sv["served_saturation"]["beam_samples_per_s"],
+                           "plain": sv["plain_saturation"]["beam_samples_per_s"]},
+            "p99_ratio_plain_over_served": sv["p99_ratio_plain_over_served"],
+            "saturation_speedup": sv["saturation_speedup"],
+            "mismatches": sum(sv[k]["mismatches"] for k in ("served", "plain_loop", "served_saturation",
+                                                            "plain_saturation")),
+            "clocks": sv.get("clocks")}
+
+    def wide():
+        a = copy.copy(args)
+        a.rounds = 3
+        w = run_wide(a, emit=False)
+        return {
+            "workload": w["config"]["workload"], "value": w["value"], "unit": w["unit"],
+            "ms_per_chunk": w["ms_per_step"], "kernel_roofline_frac": w["roofline"]["frac"],
+            "roofline_bound": w["roofline"]["bound"], "kernel_ms": w["roofline"].get("kernel_ms"),
+            "weight_updates": w["served"]["weight_updates"], "mismatches": w["mismatches"],
+            "clocks": w.get("clocks")}
+
     out = {}
-    a = copy.copy(args)
-    a.steps, a.warmup = 20, 3
-    b = run_batched(a, emit=False)
-    out["batched"] = {
-        "workload": b["config"]["workload"], "value": b["value"], "unit": b["unit"], "ms_per_step": b["ms_per_step"],
-        "roofline_frac": b["roofline"]["frac"], "roofline_bound": b["roofline"]["bound"],
-        "speedup_vs_per_problem": b["speedup_vs_per_problem"],
-        "launches": [(L["problems"], L["max_nb_pass"], L["ctas_per_sm"]) for L in b["autotune"]["launches"]],
-        "parity": b["parity"]}
-    a = copy.copy(args)
-    a.duration, a.repeats, a.extra_rates = 10.0, 1, []
-    sv = run_served(a, emit=False)
-
-    def lat(r):
-        return {q: r["latency_ms"][q] for q in ("p50", "p99", "p99.9")}
-
-    out["served"] = {
-        "workload": sv["config"]["workload"].replace("for 30 s", "for 10 s"), "unit": "beam samples/s",
-        "served": {"latency_ms": lat(sv["served"]), "beam_samples_per_s": sv["served"]["beam_samples_per_s"]},
-        "plain": {"latency_ms": lat(sv["plain_loop"]), "beam_samples_per_s": sv["plain_loop"]["beam_samples_per_s"]},
-        "saturation": {"served": sv["served_saturation"]["beam_samples_per_s"],
-                       "plain": sv["plain_saturation"]["beam_samples_per_s"]},
-        "p99_ratio_plain_over_served": sv["p99_ratio_plain_over_served"],
-        "saturation_speedup": sv["saturation_speedup"],
-        "mismatches": sum(sv[k]["mismatches"] for k in ("served", "plain_loop", "served_saturation",
-                                                        "plain_saturation")),
-        "clocks": sv.get("clocks")}
-    a = copy.copy(args)
-    a.rounds = 3
-    w = run_wide(a, emit=False)
-    out["wide"] = {
-        "workload": w["config"]["workload"], "value": w["value"], "unit": w["unit"], "ms_per_chunk": w["ms_per_step"],
-        "kernel_roofline_frac": w["roofline"]["frac"], "roofline_bound": w["roofline"]["bound"],
-        "kernel_ms": w["roofline"].get("kernel_ms"), "weight_updates": w["served"]["weight_updates"],
-        "mismatches": w["mismatches"], "clocks": w.get("clocks")}
-    try:
-        out["exact_fallback"] = run_exact_forms()
-    except Exception as e:  # the headline line must still print
-        out["exact_fallback"] = {"error": f"{type(e).__name__}: {e}"}
+    for name, fn in (("batched", batched), ("served", served), ("wide", wide), ("exact_fallback", run_exact_forms)):
+        try:
+            out[name] = fn()
+        except Exception as e:
+            out[name] = {"error": f"{type(e).__name__}: {e}"}
     return out
 
 
