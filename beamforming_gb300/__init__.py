@@ -345,11 +345,15 @@ def stream_status(stream=None) -> None:
 def plan_rings(ndishes: int, max_nb_pass: int, wslots: int = 0, raw: int = 0) -> dict | None:
     """The ring layout the tensor-core kernel plans (host only, no GPU), or
     None where no layout fits: TMEM stages, W slots, raw E slots, unpack
-    groups, CTAs per SM and K stages per tile."""
-    out = (ctypes.c_int * 6)()
+    groups, CTAs per SM, K stages per tile, and the resources: shared memory
+    bytes per CTA and the tensor-memory columns (allocated, per accumulator,
+    the second accumulator's first column, stages per accumulator and the end
+    of the stages' columns)."""
+    out = (ctypes.c_int * 12)()
     if lib().bf_plan_rings(ndishes, max_nb_pass, wslots, raw, out) != 0:
         return None
-    return dict(zip(("stages", "wslots", "raw", "groups", "ctas_per_sm", "nk"), list(out)))
+    return dict(zip(("stages", "wslots", "raw", "groups", "ctas_per_sm", "nk", "smem_bytes", "tmem_cols",
+                     "acc_cols", "acc2_col", "stages_per_acc", "stage_end_col"), list(out)))
 
 
 def set_kernel(kind: str) -> None:

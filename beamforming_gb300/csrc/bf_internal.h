@@ -172,8 +172,11 @@ int tc_stages_per_tile(int64_t D);
 cudaError_t launch_tc_grouped(const TcProblem *table, int nprob, int ntiles, int64_t D, int max_nb_pass,
                               const TcRingPlan &plan, int *err, cudaStream_t s);
 
-// The whole ring layout of a launch with these sizes: out[0..5] = stages,
-// W slots, raw E slots, unpack groups, CTAs per SM, K stages per tile.
+// The whole ring layout of a launch with these sizes: out[0..11] = stages,
+// W slots, raw E slots, unpack groups, CTAs per SM, K stages per tile,
+// dynamic shared memory bytes, TMEM columns allocated, accumulator columns,
+// column of the second accumulator, stages beside each accumulator, one past
+// the last TMEM column a stage uses.
 cudaError_t tc_plan_rings(int64_t D, int max_nb_pass, const TcRingPlan &plan, int *out);
 
 // TMEM stages, unpack groups and CTAs per SM of a grouped launch with these sizes.

@@ -1123,12 +1123,24 @@ cudaError_t tc_plan_rings(int64_t D, int max_nb_pass, const TcRingPlan &plan, in
   int smem_bytes = 0;
   const cudaError_t e = plan_launch(p, max_nb_pass, plan, &smem_bytes);
   if (e != cudaSuccess) return e;
+  const int acc = p.half ? kAccColsHalf : kAccCols;  // the kernel's kAcc
+  const int ncols = 2 * max_nb_pass;
+  const int per_half = (acc - ncols) / kStageCols;
+  int last_col = 0;  // one past the highest TMEM column an unpacked stage uses
+  for (int i = 0; i < p.stages; ++i)
+    last_col = std::max(last_col, static_cast<int>(stage_col(i, ncols, per_half, acc)) + kStageCols);
   out[0] = p.stages;
   out[1] = p.wslots;
   out[2] = p.raw;
   out[3] = p.groups;
   out[4] = p.half ? 2 : 1;
   out[5] = p.nk;
+  out[6] = smem_bytes;
+  out[7] = 2 * acc;  // TMEM columns allocated
+  out[8] = ncols;    // columns of each accumulator (at 0 and at acc)
+  out[9] = acc;
+  out[10] = per_half;
+  out[11] = last_col;
   return cudaSuccess;
 }
 

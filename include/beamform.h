@@ -195,9 +195,12 @@ BF_API int bf_batch_destroy(bf_batch *batch);
 
 /* The ring layout the tensor-core kernel plans for a launch over ndishes
  * dishes whose widest beam pass has max_nb_pass beams, with wslots W slots
- * and raw raw-E slots asked for (0: the planner's choice).  out[0..5] =
+ * and raw raw-E slots asked for (0: the planner's choice).  out[0..11] =
  * unpacked stages in tensor memory, W slots, raw E slots, unpack warp
- * groups, CTAs per SM, K stages per tile.  Host only: needs no GPU.
+ * groups, CTAs per SM, K stages per tile, dynamic shared memory bytes per
+ * CTA, tensor-memory columns allocated per CTA, columns of each accumulator,
+ * column of the second accumulator, stages beside each accumulator, one past
+ * the last column a stage uses.  Host only: needs no GPU.
  * BF_ERR_INVALID_ARGUMENT where no layout fits.  No counterpart in the
  * reference. */
 BF_API int bf_plan_rings(int64_t ndishes, int max_nb_pass, int wslots, int raw, int *out);

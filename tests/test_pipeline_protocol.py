@@ -453,6 +453,42 @@ def test_every_planned_layout_passes_the_model(bflib):
                 Model(ntiles=5, rng=rng, **cfg).run(inorder_commits=bool(seed % 2), fail=fail)
 
 
+SMEM_PER_SM = 233472  # 228 KiB of shared memory per SM
+SMEM_PER_CTA = 232448  # 227 KiB opt-in per block
+SMEM_RESERVED_PER_CTA = 1024
+TMEM_COLS_PER_SM = 512
+
+
+def test_every_planned_layout_fits_the_hardware(bflib):
+    """Every layout the planner gives stays inside the SM: shared memory per
+    CTA and per SM (two CTAs in the half-SM layout), a tensor-memory
+    allocation of a power of two >= 32 columns whose CTAs fit the SM's 512,
+    and unpacked stages whose columns overlap neither accumulator nor each
+    other."""
+    for D in (8, 64, 128, 192, 512, 1024, 2048):
+        for nb in range(8, 97, 8):
+            for wslots, raw in ((0, 0), (4, 8), (2, 12), (6, 16), (2, 2)):
+                pl = bflib.plan_rings(D, nb, wslots, raw)
+                if pl is None:
+                    continue
+                what = (D, nb, wslots, raw, pl)
+                n = pl["ctas_per_sm"]
+                assert pl["smem_bytes"] <= SMEM_PER_CTA, what
+                assert n * (pl["smem_bytes"] + SMEM_RESERVED_PER_CTA) <= SMEM_PER_SM, what
+                cols = pl["tmem_cols"]
+                assert cols >= 32 and cols & (cols - 1) == 0 and n * cols <= TMEM_COLS_PER_SM, what
+                acc, acc2, per = pl["acc_cols"], pl["acc2_col"], pl["stages_per_acc"]
+                assert acc == 2 * nb and acc <= acc2 and acc2 + acc <= cols, what
+                used = [(0, acc), (acc2, acc2 + acc)]
+                for i in range(pl["stages"]):
+                    c0 = acc + 64 * i if i < per else acc2 + acc + 64 * (i - per)
+                    used.append((c0, c0 + 64))
+                used.sort()
+                assert all(a[1] <= b[0] for a, b in zip(used, used[1:])), what  # no overlap
+                assert used[-1][1] <= cols and used[-1][1] >= pl["stage_end_col"], what
+                assert pl["stages"] >= 2 and pl["wslots"] >= 2 and pl["raw"] >= 2, what
+
+
 def test_planner_refuses_passes_it_cannot_hold(bflib):
     assert bflib.plan_rings(512, 104) is None  # wider than 96 beams: no TMEM room for two stages
     assert bflib.plan_rings(4096, 96) is None  # beyond the kernel's 2048 dishes
