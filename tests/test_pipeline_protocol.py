@@ -93,6 +93,10 @@ class Model:
         self.mma_issued = 0
         self.mma_done = 0
         self.acc_tile_done = {}
+        self.acc_reading = [None, None]  # tile whose accumulator the epilogue is reading
+        self.acc_read = set()            # tiles the epilogue has read
+        self.mma_skips_accempty = False  # planted mistake: start a tile without waiting for accempty
+        self.unpack_signals_early = False  # planted mistake: a_full before the TMEM stores are waited on
 
     # --------------------------------------------------------------- helpers
     def wait(self, bar, phase):
@@ -246,6 +250,13 @@ class Model:
                 return
             if self.busy("stage", s):
                 raise Hazard(f"unpack of sequence {k} writes TMEM stage {s} while the tensor core reads it")
+            # the TMEM stores take time: other roles may run before they are waited on
+            self.stage[s] = (k, False)
+            if self.unpack_signals_early:
+                self.a_full[s].arrive()
+            yield ("step", None, None)
+            if self.busy("stage", s):
+                raise Hazard(f"the tensor core reads TMEM stage {s} while the unpack of sequence {k} writes it")
             self.stage[s] = (k, True)
             if not self.fwd:
                 # one group: hand back the W slot of sequence k - S, wait for this one's
@@ -253,19 +264,22 @@ class Model:
                     self.w_empty[(k - self.S) % self.SW].arrive()
                 if not (yield self.wait(self.w_full[k % self.SW], k // self.SW)):
                     return
-            self.a_full[s].arrive()
+            if not self.unpack_signals_early:
+                self.a_full[s].arrive()
 
     def mma_thread(self):
         k = 0
         nstage = ndig = nacc = 0
         for t in range(self.nt):
             ab = t % 2
-            if t >= 2 and not (yield self.wait(self.accempty[ab], t // 2 - 1)):
+            if t >= 2 and not self.mma_skips_accempty and not (yield self.wait(self.accempty[ab], t // 2 - 1)):
                 break
             if not (yield self.wait(self.d_full[ab], t // 2)):
                 break
             if self.acc[ab] is not None and self.acc[ab][0] != t - 2:
                 raise Hazard(f"tile {t} starts accumulator {ab} holding {self.acc[ab]}")
+            if t >= 2 and (self.acc_reading[ab] is not None or t - 2 not in self.acc_read):
+                raise Hazard(f"tile {t} overwrites accumulator {ab} before the epilogue has read tile {t - 2}")
             self.acc[ab] = (t, True)
             self.mma([("dslot", ab, t)], t)
             self.commit(self.d_empty[ab])
@@ -299,6 +313,11 @@ class Model:
                 return
             if self.acc_tile_done.get(t, 0) != 1 + self.nk:
                 raise Hazard(f"epilogue reads tile {t} with {self.acc_tile_done.get(t, 0)} of {1 + self.nk} MMAs done")
+            # the TMEM loads take time: other roles may run before they are waited on
+            self.acc_reading[ab] = t
+            yield ("step", None, None)
+            self.acc_reading[ab] = None
+            self.acc_read.add(t)
             self.accempty[ab].arrive()
 
     # -------------------------------------------------------------- scheduler
@@ -332,6 +351,8 @@ class Model:
             while name not in done:
                 op = blocked[name]
                 kind, bar, phase = op
+                if kind == "step":  # a scheduling point: the scheduler resumes it
+                    return
                 if kind == "wait":
                     nwaits[name] += 1
                     if fail == (name, nwaits[name]):
@@ -351,7 +372,7 @@ class Model:
                 if n in done:
                     continue
                 kind, bar, phase = blocked[n]
-                if self.check_wait(bar, phase):
+                if kind == "step" or self.check_wait(bar, phase):
                     choices.append(("role", n, True))
                 elif kind == "wait" and err[0]:
                     choices.append(("role", n, False))  # gives up at a poll of the error word
@@ -362,7 +383,7 @@ class Model:
             if dc:
                 choices += [("commit", i, None) for i in range(1 if inorder_commits else len(dc))]
             if not choices:
-                raise Hazard(f"deadlock: blocked {[(n, blocked[n][1].name, blocked[n][2]) for n in roles if n not in done]}")
+                raise Hazard(f"deadlock: blocked {[(n, getattr(blocked[n][1], 'name', None), blocked[n][2]) for n in roles if n not in done]}")
             kind, i, val = self.rng.choice(choices)
             if kind == "role":
                 resume(i, val)
@@ -495,6 +516,32 @@ def test_planner_refuses_passes_it_cannot_hold(bflib):
     assert bflib.plan_rings(512, 16)["ctas_per_sm"] == 2
     assert bflib.plan_rings(512, 96)["groups"] == 1
     assert bflib.plan_rings(512, 64)["groups"] == 2
+
+
+def test_protocol_model_finds_an_accumulator_overwritten_before_it_is_read():
+    """With the MMA thread not waiting for accempty, some schedule starts a
+    tile on an accumulator the epilogue is still reading."""
+    for seed in range(200):
+        m = Model(ntiles=6, rng=random.Random(seed), **LAYOUTS["b64 two groups"])
+        m.mma_skips_accempty = True
+        try:
+            m.run()
+        except Hazard as e:
+            assert "before the epilogue has read" in str(e)
+            return
+    raise AssertionError("the planted mistake was not found")
+
+
+def test_protocol_model_finds_a_stage_signalled_before_its_stores_land():
+    for seed in range(200):
+        m = Model(ntiles=4, rng=random.Random(seed), **LAYOUTS["b64 two groups"])
+        m.unpack_signals_early = True
+        try:
+            m.run()
+        except Hazard as e:
+            assert "stage" in str(e)
+            return
+    raise AssertionError("the planted mistake was not found")
 
 
 def test_protocol_model_finds_producers_that_drain_only_on_own_errors():
