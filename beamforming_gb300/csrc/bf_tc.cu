@@ -1046,7 +1046,9 @@ static cudaError_t plan_launch(TcParams &p, int max_nb_pass, const TcRingPlan &p
   // raw slot with one group, which takes its sequences in order.
   if (groups == 2 && raw % 2 == 1) --raw;
   const int st = groups == 2 ? stages : std::min(stages, wslots);
-  if (groups == 2 && (wslots > st || raw < 2)) return cudaErrorInvalidValue;
+  // The same holds for the TMEM stage ring: stage slot k % S serves k and
+  // k + S, so two groups need an even S (here always 2 x stages per accumulator).
+  if (groups == 2 && (wslots > st || raw < 2 || st % 2 == 1)) return cudaErrorInvalidValue;
   p.max_nb_pass = max_nb_pass;
   p.stages = st;
   p.wslots = wslots;

@@ -60,7 +60,7 @@ class Hazard(AssertionError):
 class Model:
     """One CTA of the kernel over `ntiles` tiles of `nk` K stages."""
 
-    def __init__(self, S, SW, R, groups, nk, ntiles, rng, drain_always=True):
+    def __init__(self, S, SW, R, groups, nk, ntiles, rng, drain_always=True, naccs=2):
         self.S, self.SW, self.R, self.G, self.nk, self.nt = S, SW, R, groups, nk, ntiles
         # the producers drain their copies on every exit (False: only after an
         # error of their own, which leaves copies landing after the exit)
@@ -76,8 +76,12 @@ class Model:
         self.w_empty = [B(f"w_empty{i}", 1) for i in range(SW)]
         self.a_full = [B(f"a_full{i}", 1 + (1 if fwd else 0)) for i in range(S)]
         self.empty = [B(f"empty{i}", 1) for i in range(S)]
-        self.accfull = [B(f"accfull{i}", 1) for i in range(2)]
-        self.accempty = [B(f"accempty{i}", 1) for i in range(2)]
+        # accumulators in TMEM: the kernel double-buffers them (2); 1 is the
+        # candidate layout whose epilogue releases its accumulator right after
+        # reading it
+        self.A = naccs
+        self.accfull = [B(f"accfull{i}", 1) for i in range(naccs)]
+        self.accempty = [B(f"accempty{i}", 1) for i in range(naccs)]
         self.d_full = [B(f"d_full{i}", 1) for i in range(2)]
         self.d_empty = [B(f"d_empty{i}", 1) for i in range(2)]
         # slot contents: (what, id, complete?) and in-flight readers
@@ -85,7 +89,7 @@ class Model:
         self.wslot = [None] * SW
         self.dslot = [None] * 2
         self.stage = [None] * S
-        self.acc = [None] * 2
+        self.acc = [None] * naccs
         self.readers = {}  # (kind, index) -> set of in-flight reader ids
         self.events = []   # asynchronous completions: callables
         self.mma_queue = []  # in-flight MMAs in issue order: (reads, write, id)
@@ -93,7 +97,7 @@ class Model:
         self.mma_issued = 0
         self.mma_done = 0
         self.acc_tile_done = {}
-        self.acc_reading = [None, None]  # tile whose accumulator the epilogue is reading
+        self.acc_reading = [None] * naccs  # tile whose accumulator the epilogue is reading
         self.acc_read = set()            # tiles the epilogue has read
         self.mma_skips_accempty = False  # planted mistake: start a tile without waiting for accempty
         self.unpack_signals_early = False  # planted mistake: a_full before the TMEM stores are waited on
@@ -270,19 +274,20 @@ class Model:
     def mma_thread(self):
         k = 0
         nstage = ndig = nacc = 0
+        A = self.A
         for t in range(self.nt):
-            ab = t % 2
-            if t >= 2 and not self.mma_skips_accempty and not (yield self.wait(self.accempty[ab], t // 2 - 1)):
+            ab, dd = t % A, t % 2  # accumulator, digit-row slot
+            if t >= A and not self.mma_skips_accempty and not (yield self.wait(self.accempty[ab], t // A - 1)):
                 break
-            if not (yield self.wait(self.d_full[ab], t // 2)):
+            if not (yield self.wait(self.d_full[dd], t // 2)):
                 break
-            if self.acc[ab] is not None and self.acc[ab][0] != t - 2:
+            if self.acc[ab] is not None and self.acc[ab][0] != t - A:
                 raise Hazard(f"tile {t} starts accumulator {ab} holding {self.acc[ab]}")
-            if t >= 2 and (self.acc_reading[ab] is not None or t - 2 not in self.acc_read):
-                raise Hazard(f"tile {t} overwrites accumulator {ab} before the epilogue has read tile {t - 2}")
+            if t >= A and (self.acc_reading[ab] is not None or t - A not in self.acc_read):
+                raise Hazard(f"tile {t} overwrites accumulator {ab} before the epilogue has read tile {t - A}")
             self.acc[ab] = (t, True)
-            self.mma([("dslot", ab, t)], t)
-            self.commit(self.d_empty[ab])
+            self.mma([("dslot", dd, t)], t)
+            self.commit(self.d_empty[dd])
             ndig += 1
             ok = True
             for _ in range(self.nk):
@@ -303,13 +308,13 @@ class Model:
             yield ("drain", self.empty[q % self.S], q // self.S)
         for q in range(max(0, ndig - 2), ndig):
             yield ("drain", self.d_empty[q % 2], q // 2)
-        for q in range(max(0, nacc - 2), nacc):
-            yield ("drain", self.accfull[q % 2], q // 2)
+        for q in range(max(0, nacc - A), nacc):
+            yield ("drain", self.accfull[q % A], q // A)
 
     def epilogue(self):
         for t in range(self.nt):
-            ab = t % 2
-            if not (yield self.wait(self.accfull[ab], t // 2)):
+            ab = t % self.A
+            if not (yield self.wait(self.accfull[ab], t // self.A)):
                 return
             if self.acc_tile_done.get(t, 0) != 1 + self.nk:
                 raise Hazard(f"epilogue reads tile {t} with {self.acc_tile_done.get(t, 0)} of {1 + self.nk} MMAs done")
@@ -463,7 +468,7 @@ def test_every_planned_layout_passes_the_model(bflib):
     layouts = _planned_layouts(bflib)
     assert len(layouts) >= 10
     for (S, SW, R, groups), nks in sorted(layouts.items()):
-        assert groups == 1 or (R % 2 == 0 and SW <= S), (S, SW, R, groups)  # the planner's two-group rules
+        assert groups == 1 or (R % 2 == 0 and S % 2 == 0 and SW <= S), (S, SW, R, groups)  # two-group rules
         roles = ["E", "W", "MMA", "epi", "unpack0"] + (["unpack1", "fwd"] if groups > 1 else [])
         for nk in sorted(set(nks) | {1, 2, 3, 8}):
             cfg = dict(S=S, SW=SW, R=R, groups=groups, nk=min(nk, 8))
@@ -516,6 +521,37 @@ def test_planner_refuses_passes_it_cannot_hold(bflib):
     assert bflib.plan_rings(512, 16)["ctas_per_sm"] == 2
     assert bflib.plan_rings(512, 96)["groups"] == 1
     assert bflib.plan_rings(512, 64)["groups"] == 2
+
+
+@pytest.mark.parametrize("S,SW,R", [(4, 4, 4), (4, 2, 8), (4, 4, 8), (6, 4, 6)])
+def test_one_accumulator_candidate_layout(S, SW, R):
+    """The candidate b=96 layout (one accumulator released right after the
+    epilogue reads it, four stages, two unpack groups and the W forwarder):
+    no hazard, deadlock or alias under random schedules and injected
+    failures, before any of it is built."""
+    roles = ["E", "W", "MMA", "epi", "unpack0", "unpack1", "fwd"]
+    for seed in range(60):
+        rng = random.Random(_seed("one acc", S, SW, R, seed))
+        cfg = dict(S=S, SW=SW, R=R, groups=2, nk=4, naccs=1)
+        Model(ntiles=6, rng=rng, **cfg).run(inorder_commits=bool(seed % 2))
+        Model(ntiles=6, rng=rng, **cfg).run(fail=(rng.choice(roles), rng.randint(1, 12)))
+
+
+def test_protocol_model_finds_odd_stage_rings_with_two_groups():
+    """Stage slot k % S serves sequences k and k + S; with an odd S they
+    belong to different unpack groups, and the group with k + S can pass its
+    `empty` parity wait one phase early, as with an odd raw ring.  The
+    planner's stage counts are even (two per accumulator times the stages
+    beside each); the one-accumulator candidate must keep S even too (four
+    stages at b=96, not the five its TMEM would hold)."""
+    for seed in range(300):  # found only when commit arrivals may land out of order (undocumented either way)
+        try:
+            Model(ntiles=6, rng=random.Random(seed), S=5, SW=4, R=6, groups=2, nk=4, naccs=1).run(
+                inorder_commits=False)
+        except Hazard as e:
+            assert "empty" in str(e)
+            return
+    raise AssertionError("the odd stage ring was not found")
 
 
 def test_protocol_model_finds_an_accumulator_overwritten_before_it_is_read():
