@@ -445,6 +445,16 @@ int finish_adler(DeviceCtx &c, bool fused, const uint8_t *Jdev, size_t n, cudaSt
   return BF_OK;
 }
 
+// After a failed synchronous host-pointer call: wait for what it had already
+// queued (copies from the caller's E, drains into the caller's J) so that
+// nothing touches the caller's buffers once the call has returned.
+void settle_after_error(DeviceCtx &c, cudaStream_t s) {
+  (void)cudaStreamSynchronize(s);
+  if (c.lanes_ready)
+    for (Lane &l : c.lanes) (void)cudaStreamSynchronize(l.s);
+  (void)cudaGetLastError();
+}
+
 }  // namespace
 }  // namespace bf
 
@@ -482,27 +492,31 @@ static int form_beams_impl(const bf_dims *dims, uint8_t *J, const uint8_t *E, co
 
   // Host pointers: stage in, compute, stage out, synchronously (cuda.cu:274-314 does the same around its
   // kernel), pipelined over time chunks when there is more than one.
-  if (chunk_times(d) < d.ntimes) {
-    st = run_host_pipelined(*c, d, J, E, A, G, s, a_layout, j_layout, adl, &fused);
-    if (st != BF_OK || !adler_out) return st;
-    return finish_adler(*c, fused, c->J.as<uint8_t>(), jsize(d), s, adler_out);
-  }
-  BF_TRY(c->E.reserve(esize(d)));
-  BF_TRY(c->A.reserve(asize(d)));
-  BF_TRY(c->G.reserve(gsize(d) * sizeof(float)));
-  BF_TRY(c->J.reserve(jsize(d)));
-  BF_TRY(cudaMemcpyAsync(c->E.p, E, esize(d), cudaMemcpyHostToDevice, s));
-  BF_TRY(cudaMemcpyAsync(c->A.p, A, asize(d), cudaMemcpyHostToDevice, s));
-  BF_TRY(cudaMemcpyAsync(c->G.p, G, gsize(d) * sizeof(float), cudaMemcpyHostToDevice, s));
-  st = run_device(*c, d, c->J.as<uint8_t>(), c->E.as<uint8_t>(), c->A.as<uint8_t>(), c->G.as<float>(), s, a_layout,
-                  j_layout, adl, &fused);
-  if (st != BF_OK) return st;
-  BF_TRY(cudaMemcpyAsync(J, c->J.p, jsize(d), cudaMemcpyDeviceToHost, s));
-  if (adler_out) {
-    st = finish_adler(*c, fused, c->J.as<uint8_t>(), jsize(d), s, adler_out);
-    if (st != BF_OK) return st;
-  }
-  return read_and_clear_err(*c, s);
+  const int hs = [&]() -> int {
+    if (chunk_times(d) < d.ntimes) {
+      const int ps = run_host_pipelined(*c, d, J, E, A, G, s, a_layout, j_layout, adl, &fused);
+      if (ps != BF_OK || !adler_out) return ps;
+      return finish_adler(*c, fused, c->J.as<uint8_t>(), jsize(d), s, adler_out);
+    }
+    BF_TRY(c->E.reserve(esize(d)));
+    BF_TRY(c->A.reserve(asize(d)));
+    BF_TRY(c->G.reserve(gsize(d) * sizeof(float)));
+    BF_TRY(c->J.reserve(jsize(d)));
+    BF_TRY(cudaMemcpyAsync(c->E.p, E, esize(d), cudaMemcpyHostToDevice, s));
+    BF_TRY(cudaMemcpyAsync(c->A.p, A, asize(d), cudaMemcpyHostToDevice, s));
+    BF_TRY(cudaMemcpyAsync(c->G.p, G, gsize(d) * sizeof(float), cudaMemcpyHostToDevice, s));
+    const int rs = run_device(*c, d, c->J.as<uint8_t>(), c->E.as<uint8_t>(), c->A.as<uint8_t>(), c->G.as<float>(),
+                              s, a_layout, j_layout, adl, &fused);
+    if (rs != BF_OK) return rs;
+    BF_TRY(cudaMemcpyAsync(J, c->J.p, jsize(d), cudaMemcpyDeviceToHost, s));
+    if (adler_out) {
+      const int as = finish_adler(*c, fused, c->J.as<uint8_t>(), jsize(d), s, adler_out);
+      if (as != BF_OK) return as;
+    }
+    return read_and_clear_err(*c, s);
+  }();
+  if (hs != BF_OK) settle_after_error(*c, s);
+  return hs;
 }
 
 extern "C" {
