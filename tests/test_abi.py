@@ -148,3 +148,36 @@ def test_no_device_reported(bflib):
     with pytest.raises(bflib.BeamformError) as ei:
         bflib.form_beams_ex(d, J, E, A, G)
     assert ei.value.status == bflib.ERR_NO_DEVICE
+
+
+def test_every_entry_point_checks_its_arguments_before_the_device(bflib):
+    """Null handles and pointers, and impossible sizes, are refused by every
+    entry point without a device; empty work succeeds."""
+    L = bflib.lib()
+    E = bflib.ERR_INVALID_ARGUMENT
+    h = ctypes.c_void_p()
+    d = bflib.Dims(4, 1, 8, 2, 8).c()
+    d0 = bflib.Dims(0, 1, 8, 2, 8).c()
+    assert L.bf_weights_create(None, 1, 8, 8, None, None, 0, None) == E
+    assert L.bf_weights_create(ctypes.byref(h), 0, 8, 8, None, None, 0, None) == E
+    assert L.bf_weights_update(None, None, None, 0, None) == E
+    assert L.bf_weights_destroy(None) == bflib.OK
+    assert L.bf_form_beams_resident(None, 0, None, None, 16, None) == E
+    assert L.bf_form_beams_noalloc(None, None, None, None, None, None) == E
+    assert L.bf_form_beams_noalloc(ctypes.byref(d), None, None, None, None, None) == E
+    assert L.bf_form_beams_noalloc(ctypes.byref(d0), None, None, None, None, None) == bflib.OK
+    assert L.bf_batch_create(None, None, 0, None) == E
+    assert L.bf_batch_run(None, None) == E
+    assert L.bf_batch_info(None, None, None, None, None, None) == E
+    assert L.bf_batch_shape(None, None, None, None, None, None, None, None) == E
+    assert L.bf_batch_destroy(None) == bflib.OK
+    assert L.bf_server_update_weights(None, None, None, 0) == E
+    assert L.bf_server_stats_get(None, None) == E
+    assert L.bf_fill_random_host(None, 4, 1, 0) == E
+    assert L.bf_fill_random_host(None, 0, 1, 0) == bflib.OK
+    assert L.bf_fill_random_device(None, 4, 1, 0, None) == E
+    assert L.bf_gains_host(None, None) == E
+    out = (ctypes.c_int * 12)()
+    assert L.bf_plan_rings(0, 8, 0, 0, out) == E
+    assert L.bf_plan_rings(512, 8, 0, 0, None) == E
+    assert L.bf_plan_rings(512, 96, 0, 0, out) == bflib.OK
