@@ -62,6 +62,7 @@ EXPORTED_SYMBOLS = (
     "bf_batch_shape",
     "bf_batch_destroy",
     "bf_tensor_peak",
+    "bf_dp4a_peak",
     "bf_form_beams_layout",
     "bf_server_create",
     "bf_server_submit",
@@ -186,6 +187,7 @@ def lib() -> ctypes.CDLL:
         L.bf_server_submit.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int64, u8p, ctypes.c_int, u8p,
                                        ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]
         L.bf_tensor_peak.argtypes = [ctypes.POINTER(ctypes.c_double), vp]
+        L.bf_dp4a_peak.argtypes = [ctypes.POINTER(ctypes.c_double), vp]
         L.bf_server_update_weights.argtypes = [vp, u8p, fp, ctypes.c_int]
         L.bf_server_wait.argtypes = [vp, ctypes.c_int64, ctypes.POINTER(ctypes.c_double)]
         L.bf_server_drain.argtypes = [vp]
@@ -606,6 +608,13 @@ def tensor_peak_tflops(stream=None) -> float:
     """Measured dense E4M3 tcgen05 MMA rate of the current device (TFLOP/s)."""
     out = ctypes.c_double()
     _check(lib().bf_tensor_peak(ctypes.byref(out), _stream_handle(stream)), "bf_tensor_peak")
+    return out.value
+
+
+def dp4a_peak_per_s(stream=None) -> float:
+    """Measured CUDA-core dp4a rate of the current device (lane operations/s)."""
+    out = ctypes.c_double()
+    _check(lib().bf_dp4a_peak(ctypes.byref(out), _stream_handle(stream)), "bf_dp4a_peak")
     return out.value
 
 

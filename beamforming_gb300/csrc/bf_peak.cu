@@ -1,4 +1,5 @@
-// bf_peak.cu -- the dense E4M3 tensor-core rate of this GPU, measured.
+// bf_peak.cu -- the dense E4M3 tensor-core rate and the CUDA-core dp4a rate
+// of this GPU, measured.
 //
 // The roofline of the beamformer's tensor-core kernel is the rate at which
 // the SMs retire `tcgen05.mma.kind::f8f6f4` with the A operand in tensor
@@ -67,10 +68,74 @@ __global__ void __launch_bounds__(128, 1) bf_tensor_peak_kernel(int reps, int *e
   }
 }
 
+// The CUDA-core dp4a rate, the instruction of the exact kernel: every thread
+// runs kDpChains independent dp4a chains (enough to cover the pipe latency)
+// with per-chain operands that change every step, and stores one word so
+// that nothing is eliminated.
+constexpr int kDpChains = 16;  // loop overhead about 1 instruction in 16
+constexpr int kDpThreads = 256;
+constexpr int kDpBlocksPerSm = 8;
+
+__global__ void __launch_bounds__(kDpThreads) bf_dp4a_peak_kernel(int reps, uint32_t *out) {
+  int a[kDpChains], acc[kDpChains];
+#pragma unroll
+  for (int j = 0; j < kDpChains; ++j) {
+    a[j] = static_cast<int>((0x01020304u ^ threadIdx.x) + 0x01010101u * j);
+    acc[j] = j;
+  }
+  int b = static_cast<int>(0x05060708u + blockIdx.x);
+  for (int i = 0; i < reps; ++i) {
+#pragma unroll
+    for (int j = 0; j < kDpChains; ++j) acc[j] = __dp4a(a[j], b, acc[j]);
+    b ^= i;
+  }
+  uint32_t x = 0;
+#pragma unroll
+  for (int j = 0; j < kDpChains; ++j) x ^= static_cast<uint32_t>(acc[j]);
+  out[static_cast<size_t>(blockIdx.x) * kDpThreads + threadIdx.x] = x;
+}
+
 }  // namespace
 }  // namespace bf
 
 using namespace bf;
+
+extern "C" int bf_dp4a_peak(double *dp4a_per_s, bf_stream_t stream) {
+  if (!dp4a_per_s) return BF_ERR_INVALID_ARGUMENT;
+  *dp4a_per_s = 0.0;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+    return BF_ERR_NO_DEVICE;
+  const int blocks = sms * kDpBlocksPerSm;
+  uint32_t *out = nullptr;
+  if (cudaMalloc(&out, sizeof(uint32_t) * static_cast<size_t>(blocks) * kDpThreads) != cudaSuccess)
+    return BF_ERR_OUT_OF_MEMORY;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int reps = 1 << 13;  // about 1-2 ms per launch
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int st = BF_OK;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) st = BF_ERR_CUDA;
+  float best = -1.0f;
+  for (int rep = 0; rep < 6 && st == BF_OK; ++rep) {
+    cudaEventRecord(e0, s);
+    bf_dp4a_peak_kernel<<<blocks, kDpThreads, 0, s>>>(reps, out);
+    cudaEventRecord(e1, s);
+    if (cudaGetLastError() != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
+      st = BF_ERR_CUDA;
+      break;
+    }
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (rep > 0 && (best < 0.0f || ms < best)) best = ms;  // the first launch warms up
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(out);
+  if (st != BF_OK) return st;
+  *dp4a_per_s = static_cast<double>(blocks) * kDpThreads * reps * kDpChains / (best * 1e-3);
+  return BF_OK;
+}
 
 extern "C" int bf_tensor_peak(double *tflops, bf_stream_t stream) {
   if (!tflops) return BF_ERR_INVALID_ARGUMENT;

@@ -813,6 +813,17 @@ def run_exact_forms(reps=3):
             out[name] = {"ms": round(ms, 3), "value": d.cmacs / (ms * 1e-3), "adler32_equals_tensor": ok}
     finally:
         bf.set_kernel("auto")
+    # roofline of this kernel: the dp4a rate measured now (3 int8 MACs per
+    # complex MAC in the Gauss form, 4 in the 4-multiply form; 4 per dp4a)
+    try:
+        peak = bf.dp4a_peak_per_s(stream)
+    except Exception:
+        peak = None
+    out["dp4a_peak_per_s"] = peak
+    for name, per_cmac in (("gauss", 0.75), ("four_multiply", 1.0)):
+        rate = d.cmacs * per_cmac / (out[name]["ms"] * 1e-3)
+        out[name]["dp4a_per_s"] = rate
+        out[name]["dp4a_frac"] = round(rate / peak, 4) if peak else None
     golden = golden_full_adler32()
     out["adler32"] = f"{want:#010x}"
     out["adler32_equals_reference_cpu"] = None if golden is None else want == golden

@@ -240,6 +240,12 @@ BF_API int bf_form_beams_adler(const bf_dims *dims, uint8_t *J, const uint8_t *E
  * the tensor roofline the benchmarks report fractions of; takes ~15 ms. */
 BF_API int bf_tensor_peak(double *tflops, bf_stream_t stream);
 
+/* Measures the CUDA-core dp4a rate of the current device, in dp4a lane
+ * operations per second (four int8 multiply-adds each): every SM runs
+ * independent dp4a chains, timed with CUDA events.  The roofline of the exact
+ * dp4a kernel; takes a few ms. */
+BF_API int bf_dp4a_peak(double *dp4a_per_s, bf_stream_t stream);
+
 /* ---------------------------------------------------------------- serving */
 
 /* A served stream of voltage chunks with continuous batching.  No

@@ -181,3 +181,5 @@ def test_every_entry_point_checks_its_arguments_before_the_device(bflib):
     assert L.bf_plan_rings(0, 8, 0, 0, out) == E
     assert L.bf_plan_rings(512, 8, 0, 0, None) == E
     assert L.bf_plan_rings(512, 96, 0, 0, out) == bflib.OK
+    assert L.bf_dp4a_peak(None, None) == E
+    assert L.bf_tensor_peak(None, None) == E

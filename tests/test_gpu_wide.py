@@ -92,6 +92,11 @@ def test_tensor_peak_is_measured(bflib):
     assert 500.0 < tf < 20000.0
 
 
+def test_dp4a_peak_is_measured(bflib):
+    rate = bflib.dp4a_peak_per_s()
+    assert 1e12 < rate < 1e15
+
+
 def test_server_refresh_under_load(bflib, cuda):
     """Refreshes while several grouped launches are in flight (each chunk
     checked against a plain launch with the weights of its submission).  This
