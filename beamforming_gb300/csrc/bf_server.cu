@@ -137,6 +137,7 @@ struct Flight {
   std::vector<Request> reqs;
   bool busy = false;    // guarded by the server mutex
   bool landed = false;  // set by the host function behind the output copies
+  bool failed = false;  // its launch failed part-way: retired without completing its chunks
   Clock::time_point landed_at;
 };
 
@@ -259,13 +260,17 @@ bool bf_server::launch(Flight &fl, const std::vector<Request> &reqs, int *ntiles
 // still sits in the staging ring is moved to `staged` instead and completes
 // in hand_out(), which copies it to the caller without the mutex.
 void bf_server::retire_locked(Flight &fl, std::vector<Request> &staged) {
-  if (*fl.err_host != 0 && status == BF_OK) status = BF_ERR_DEVICE_TIMEOUT;  // a kernel wait gave up
+  if (!fl.failed && *fl.err_host != 0 && status == BF_OK) status = BF_ERR_DEVICE_TIMEOUT;  // a kernel wait gave up
   for (Request &r : fl.reqs) {
     --ver[r.version].refs;
     if (!r.e_on_device) pool.release(r.dE, r.e_bytes);
     if (!r.j_on_device) pool.release(r.dJ, r.j_bytes);
     if (r.sE) staging.release(r.sE, r.e_bytes);
     r.sE = nullptr;
+    if (fl.failed) {  // never completed: waits for it return the server's error status
+      if (r.sJ) staging.release(r.sJ, r.j_bytes);
+      continue;
+    }
     if (r.sJ) {
       staged.push_back(r);
       continue;
@@ -276,6 +281,7 @@ void bf_server::retire_locked(Flight &fl, std::vector<Request> &staged) {
   fl.reqs.clear();
   fl.busy = false;
   fl.landed = false;
+  fl.failed = false;
   cv_done.notify_all();
 }
 
@@ -371,13 +377,24 @@ void bf_server::run() {
         lk.unlock();
         int ntiles = 0;
         const bool ok = launch(*slot, batch, &ntiles);
+        // A launch that failed part-way records no event of its own (the
+        // flight's event still holds an earlier launch) and no host function:
+        // let what it did queue finish, then retire it as failed, so that its
+        // memory is freed and none of its chunks is reported complete.
+        if (!ok) (void)cudaStreamSynchronize(slot->s);
         lk.lock();
         slot->reqs = std::move(batch);
         const int n = static_cast<int>(slot->reqs.size());
         stats.batches += 1;
         stats.chunks_launched += n;
         stats.max_batch_seen = std::max<int64_t>(stats.max_batch_seen, n);
-        if (!ok && status == BF_OK) status = BF_ERR_CUDA;
+        if (!ok) {
+          if (status == BF_OK) status = BF_ERR_CUDA;
+          slot->failed = true;
+          slot->landed = true;
+          slot->landed_at = Clock::now();
+          cv_done.notify_all();
+        }
         hand_out(lk, staged);
         lk.unlock();
         continue;
